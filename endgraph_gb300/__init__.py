@@ -1,0 +1,332 @@
+"""endgraph_gb300 -- EndGraph preprocessing and the Gemini process_edges toolkits on one GB300.
+
+Python binding of ``libendgraph_gb300.so`` (C ABI: ``include/endgraph_gb300.h``) via ctypes.
+``Graph`` mirrors the reference's ``Graph<EdgeData>`` (core/graph.hpp:100): construct with eta,
+``load_directed`` / ``load_undirected_from_directed``, then the toolkits.  Buffers may be numpy
+arrays (host memory, copied inside the call) or CUDA torch tensors (device memory).
+
+There is no CPU path: every call runs the CUDA kernels of the shared library, and importing
+functionality fails loudly when the library is missing or no GPU is present.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = _build.LIB
+
+EG_HOST, EG_DEVICE = 0, 1
+STATUS = {0: "EG_OK", 1: "EG_ERR_INVALID", 2: "EG_ERR_CUDA", 3: "EG_ERR_NOMEM", 4: "EG_ERR_STATE",
+          5: "EG_ERR_TIMEOUT", 6: "EG_ERR_HOST_CALLBACK", 7: "EG_ERR_UNSUPPORTED"}
+
+
+class EndGraphError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("eta", ctypes.c_uint64), ("partitions", ctypes.c_int32), ("sub_partitions", ctypes.c_int32),
+                ("max_iterations", ctypes.c_int32), ("device", ctypes.c_int32), ("stream", ctypes.c_void_p)]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("V", ctypes.c_uint32), ("partitions", ctypes.c_uint32), ("E", ctypes.c_uint64),
+                ("ncompressed", ctypes.c_uint64), ("weighted", ctypes.c_int32), ("built_csr", ctypes.c_int32),
+                ("built_csc", ctypes.c_int32), ("symmetric", ctypes.c_int32)]
+
+
+class KernelStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_uint64), ("ms", ctypes.c_double)]
+
+
+# every exported symbol of include/endgraph_gb300.h with its ctypes signature
+_vp, _u32, _u64, _i32, _f32, _f64 = (ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int,
+                                      ctypes.c_float, ctypes.c_double)
+SIGNATURES = {
+    "eg_create": ([_vp, _vp], _i32),
+    "eg_destroy": ([_vp], _i32),
+    "eg_last_error": ([], ctypes.c_char_p),
+    "eg_version": ([], _i32),
+    "eg_stream": ([_vp], _vp),
+    "eg_sync": ([_vp], _i32),
+    "eg_load_edges": ([_vp, _vp, _u64, _u32, _i32, _i32, _i32], _i32),
+    "eg_build": ([_vp, _i32, _i32], _i32),
+    "eg_load_directed": ([_vp, _vp, _u64, _u32, _i32, _i32], _i32),
+    "eg_load_undirected_from_directed": ([_vp, _vp, _u64, _u32, _i32, _i32], _i32),
+    "eg_get_info": ([_vp, _vp], _i32),
+    "eg_get_partition": ([_vp, _vp, _vp], _i32),
+    "eg_get_degrees": ([_vp, _vp, _vp, _i32], _i32),
+    "eg_get_csr": ([_vp, _vp], _i32),
+    "eg_get_csc": ([_vp, _vp], _i32),
+    "eg_copy_csr": ([_vp, _vp, _vp, _vp, _vp, _i32], _i32),
+    "eg_copy_csc": ([_vp, _vp, _vp, _vp, _vp, _vp, _i32], _i32),
+    "eg_cpbt_partition": ([_vp, _u32, _i32, _i32, _u64, _i32, _i32, _i32, _vp, _vp], _i32),
+    "eg_optimal_offset": ([_vp, _u32, _u32, _vp], _i32),
+    "eg_pagerank": ([_vp, _i32, _f32, _vp, _i32], _i32),
+    "eg_bfs": ([_vp, _u32, _vp, _vp, _i32, _vp], _i32),
+    "eg_cc": ([_vp, _vp, _i32], _i32),
+    "eg_sssp": ([_vp, _u32, _vp, _i32], _i32),
+    "eg_last_run": ([_vp, _vp, _vp, _vp, _vp], _i32),
+    "eg_generate_rmat": ([_vp, _i32, _u64, _u32, _f64, _f64, _f64, _u64, _i32, _f32, _f32, _vp], _i32),
+    "eg_profile_enable": ([_vp, _i32], _i32),
+    "eg_profile_reset": ([_vp], _i32),
+    "eg_profile_read": ([_vp, _vp, _i32, _vp], _i32),
+}
+
+_lib = None
+
+
+def load_library(path: str | None = None, build_if_missing: bool = False):
+    """Load libendgraph_gb300.so (raises if it is absent and not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise EndGraphError(1, f"{path} is missing: run `python -m endgraph_gb300.build`")
+        _build.build()
+    L = ctypes.CDLL(path)
+    for name, (args, res) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != 0:
+        msg = load_library().eg_last_error()
+        raise EndGraphError(status, msg.decode() if msg else "")
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+def _buf(x):
+    """(pointer, where) of a numpy array or CUDA torch tensor; (None, host) for None."""
+    if x is None:
+        return None, EG_HOST
+    if _is_torch(x):
+        if not x.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return ctypes.c_void_p(x.data_ptr()), (EG_DEVICE if x.is_cuda else EG_HOST)
+    if not x.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return ctypes.c_void_p(x.ctypes.data), EG_HOST
+
+
+def pack_edges(src, dst, w=None):
+    """Reference binary records (core/type.hpp:29-43): u32 src, u32 dst [, f32 w], packed."""
+    E = len(src)
+    if w is None:
+        rec = np.empty((E, 2), np.uint32)
+        rec[:, 0] = src
+        rec[:, 1] = dst
+    else:
+        rec = np.empty((E, 3), np.uint32)
+        rec[:, 0] = src
+        rec[:, 1] = dst
+        rec[:, 2] = np.asarray(w, np.float32).view(np.uint32)
+    return rec
+
+
+class Graph:
+    """Graph<EdgeData> on one GPU (core/graph.hpp:100-1819)."""
+
+    def __init__(self, eta=1, partitions=1, sub_partitions=1, max_iterations=20, device=0, stream=None):
+        L = load_library()
+        self._L = L
+        cfg = Config(eta, partitions, sub_partitions, max_iterations, device, stream)
+        h = ctypes.c_void_p()
+        _check(L.eg_create(ctypes.byref(h), ctypes.byref(cfg)))
+        self.h = h
+        self.partitions = partitions
+        self.sub_partitions = sub_partitions
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.eg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- loading / preprocessing ----------------------------------------------------------------
+    @staticmethod
+    def _records(edges):
+        if _is_torch(edges):
+            rec = edges.shape[-1] * 4 if edges.dim() == 2 else None
+            n = edges.shape[0]
+            return edges, n, rec
+        edges = np.ascontiguousarray(edges)
+        return edges, edges.shape[0], edges.shape[1] * 4
+
+    def load_edges(self, edges, V, symmetric=False):
+        edges, E, rec = self._records(edges)
+        p, where = _buf(edges)
+        _check(self._L.eg_load_edges(self.h, p, E, V, rec, int(symmetric), where))
+
+    def build(self, csr=True, csc=True):
+        _check(self._L.eg_build(self.h, int(csr), int(csc)))
+
+    def load_directed(self, edges, V):
+        edges, E, rec = self._records(edges)
+        p, where = _buf(edges)
+        _check(self._L.eg_load_directed(self.h, p, E, V, rec, where))
+
+    def load_undirected_from_directed(self, edges, V):
+        edges, E, rec = self._records(edges)
+        p, where = _buf(edges)
+        _check(self._L.eg_load_undirected_from_directed(self.h, p, E, V, rec, where))
+
+    def info(self):
+        i = Info()
+        _check(self._L.eg_get_info(self.h, ctypes.byref(i)))
+        return i
+
+    @property
+    def stream(self):
+        return self._L.eg_stream(self.h)
+
+    def sync(self):
+        _check(self._L.eg_sync(self.h))
+
+    def partition(self):
+        i = self.info()
+        po = np.empty(i.partitions + 1, np.uint32)
+        lo = np.empty(i.partitions * (self.sub_partitions + 1), np.uint32)
+        _check(self._L.eg_get_partition(self.h, _buf(po)[0], _buf(lo)[0]))
+        return po, lo.reshape(i.partitions, self.sub_partitions + 1)
+
+    def degrees(self):
+        V = self.info().V
+        out = np.empty(V, np.uint32)
+        inn = np.empty(V, np.uint32)
+        _check(self._L.eg_get_degrees(self.h, _buf(out)[0], _buf(inn)[0], EG_HOST))
+        return out, inn
+
+    def csr(self):
+        i = self.info()
+        P, V, E = i.partitions, i.V, i.E
+        off = np.empty(P * (V + 1), np.uint64)
+        adj = np.empty(max(E, 1), np.uint32)
+        w = np.empty(max(E, 1), np.float32) if i.weighted else None
+        bm = np.empty(P * (V // 64 + 1), np.uint64)
+        _check(self._L.eg_copy_csr(self.h, _buf(off)[0], _buf(adj)[0], _buf(w)[0], _buf(bm)[0], EG_HOST))
+        return dict(off=off.reshape(P, V + 1), adj=adj[:E], w=None if w is None else w[:E],
+                    bitmap=bm.reshape(P, V // 64 + 1))
+
+    def csc(self):
+        i = self.info()
+        P, V, E, n = i.partitions, i.V, i.E, i.ncompressed
+        off = np.empty(P * (V + 1), np.uint64)
+        adj = np.empty(max(E, 1), np.uint32)
+        w = np.empty(max(E, 1), np.float32) if i.weighted else None
+        cv = np.empty(max(n, 1), np.uint32)
+        ci = np.empty(max(n, 1), np.uint64)
+        _check(self._L.eg_copy_csc(self.h, _buf(off)[0], _buf(adj)[0], _buf(w)[0], _buf(cv)[0], _buf(ci)[0],
+                                   EG_HOST))
+        return dict(off=off.reshape(P, V + 1), adj=adj[:E], w=None if w is None else w[:E], cvert=cv[:n],
+                    cidx=ci[:n])
+
+    # ---- toolkits ------------------------------------------------------------------------------
+    def pagerank(self, iterations=20, damping=0.85, out=None):
+        if out is None:
+            out = np.empty(self.info().V, np.float32)
+        p, where = _buf(out)
+        _check(self._L.eg_pagerank(self.h, iterations, damping, p, where))
+        return out
+
+    def bfs(self, root, level=None, parent=None, want_parent=True):
+        V = self.info().V
+        if level is None:
+            level = np.empty(V, np.uint32)
+        if parent is None and want_parent:
+            parent = np.empty(V, np.uint32)
+        pl, where = _buf(level)
+        pp, _ = _buf(parent)
+        reached = ctypes.c_uint64()
+        _check(self._L.eg_bfs(self.h, root, pl, pp, where, ctypes.byref(reached)))
+        return level, parent
+
+    def cc(self, label=None):
+        if label is None:
+            label = np.empty(self.info().V, np.uint32)
+        p, where = _buf(label)
+        _check(self._L.eg_cc(self.h, p, where))
+        return label
+
+    def sssp(self, root, dist=None):
+        if dist is None:
+            dist = np.empty(self.info().V, np.float32)
+        p, where = _buf(dist)
+        _check(self._L.eg_sssp(self.h, root, p, where))
+        return dist
+
+    def last_run(self):
+        e = ctypes.c_uint64()
+        it, pu, pl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(self._L.eg_last_run(self.h, ctypes.byref(e), ctypes.byref(it), ctypes.byref(pu), ctypes.byref(pl)))
+        return dict(edges=e.value, iterations=it.value, push=pu.value, pull=pl.value)
+
+    # ---- profiling ------------------------------------------------------------------------------
+    def profile(self, enable=True):
+        _check(self._L.eg_profile_enable(self.h, int(enable)))
+
+    def profile_reset(self):
+        _check(self._L.eg_profile_reset(self.h))
+
+    def profile_read(self):
+        n = ctypes.c_int()
+        _check(self._L.eg_profile_read(self.h, None, 0, ctypes.byref(n)))
+        arr = (KernelStat * max(n.value, 1))()
+        _check(self._L.eg_profile_read(self.h, arr, n.value, ctypes.byref(n)))
+        return {arr[i].name.decode(): (arr[i].launches, arr[i].ms) for i in range(n.value)}
+
+
+def cpbt_partition(deg, V, P, S=1, eta=1, max_iterations=20, dense=True):
+    """assign_vertices boundaries (core/graph.hpp:662-792) computed on the GPU."""
+    L = load_library()
+    po = np.empty(P + 1, np.uint32)
+    lo = np.empty(P * (S + 1), np.uint32)
+    p, where = _buf(deg)
+    _check(L.eg_cpbt_partition(p, V, P, S, eta, max_iterations, int(dense), where, _buf(po)[0], _buf(lo)[0]))
+    return po, lo.reshape(P, S + 1)
+
+
+def optimal_offset(a, k):
+    """optimal_offset(a, n, k) (core/graph.hpp:597-626) on the GPU."""
+    L = load_library()
+    a = np.ascontiguousarray(a, np.uint64)
+    out = np.empty(k + 1, np.uint32)
+    _check(L.eg_optimal_offset(_buf(a)[0] if len(a) else None, len(a), k, _buf(out)[0]))
+    return out
+
+
+def generate_rmat(out, V, E, seed, a=0.57, b=0.19, c=0.19, permute=True, weights=None, stream=None):
+    """Fill a CUDA tensor of shape (E, 2) or (E, 3) (uint32/int32 storage) with R-MAT records."""
+    L = load_library()
+    rec = out.shape[1] * 4
+    lo, hi = weights or (0.0, 1.0)
+    _check(L.eg_generate_rmat(ctypes.c_void_p(out.data_ptr()), rec, E, V, a, b, c, seed, int(permute), lo, hi,
+                              stream))
+    return out

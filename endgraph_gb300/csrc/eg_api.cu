@@ -1,0 +1,370 @@
+// eg_api.cu — the extern "C" boundary of libendgraph_gb300.so (include/endgraph_gb300.h).
+#include <string.h>
+
+#include <algorithm>
+#include <memory>
+
+#include "eg_common.cuh"
+
+using namespace eg;
+
+namespace {
+
+int check_graph(eg_graph* g, const char* fn) {
+    if (!g) {
+        set_error("%s: null handle", fn);
+        return EG_ERR_INVALID;
+    }
+    cudaError_t e = cudaSetDevice(g->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice", __FILE__, __LINE__);
+    return EG_OK;
+}
+
+int init_handle(eg_graph* g, const eg_config* cfg) {
+    eg_config c = {1, 1, 1, 20, 0, nullptr};
+    if (cfg) c = *cfg;
+    if (c.partitions < 1 || c.partitions > kMaxPartitions) {
+        set_error("eg_create: partitions must be in [1, %d]", kMaxPartitions);
+        return EG_ERR_INVALID;
+    }
+    if (c.sub_partitions < 1 || c.sub_partitions > kMaxPartitions) {
+        set_error("eg_create: sub_partitions must be in [1, %d]", kMaxPartitions);
+        return EG_ERR_INVALID;
+    }
+    int ndev = 0;
+    EG_CUDA(cudaGetDeviceCount(&ndev));
+    if (c.device < 0 || c.device >= ndev) {
+        set_error("eg_create: device %d not present (%d devices)", c.device, ndev);
+        return EG_ERR_INVALID;
+    }
+    g->device = c.device;
+    EG_CUDA(cudaSetDevice(g->device));
+    g->eta = c.eta;
+    g->partitions = c.partitions;
+    g->sub_partitions = c.sub_partitions;
+    g->max_iterations = c.max_iterations;
+    if (c.stream) {
+        g->stream = (cudaStream_t)c.stream;
+        g->own_stream = false;
+    } else {
+        EG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+        g->own_stream = true;
+    }
+    EG_TRY(g->err.reserve(64));
+    EG_CUDA(cudaMemsetAsync(g->err.ptr, 0, 64, g->stream));
+    return EG_OK;
+}
+
+void free_handle(eg_graph* g) {
+    if (!g) return;
+    cudaSetDevice(g->device);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    g->prof.clear();
+    if (g->pinned) cudaFreeHost(g->pinned);
+    cudaStream_t s = g->stream;
+    bool own = g->own_stream;
+    delete g;  // DevBuf destructors free device memory
+    if (own && s) cudaStreamDestroy(s);
+}
+
+struct HandleDeleter {
+    void operator()(eg_graph* g) const { free_handle(g); }
+};
+
+}  // namespace
+
+extern "C" {
+
+int eg_version(void) { return 1; }
+
+const char* eg_last_error(void) { return error_text(); }
+
+int eg_create(eg_graph** out, const eg_config* cfg) {
+    if (!out) {
+        set_error("eg_create: null output");
+        return EG_ERR_INVALID;
+    }
+    *out = nullptr;
+    eg_graph* g = new eg_graph();
+    int s = init_handle(g, cfg);
+    if (s != EG_OK) {
+        free_handle(g);
+        return s;
+    }
+    *out = g;
+    return EG_OK;
+}
+
+int eg_destroy(eg_graph* g) {
+    if (!g) return EG_OK;
+    free_handle(g);
+    return EG_OK;
+}
+
+void* eg_stream(eg_graph* g) { return g ? (void*)g->stream : nullptr; }
+
+int eg_sync(eg_graph* g) {
+    EG_TRY(check_graph(g, "eg_sync"));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    return EG_OK;
+}
+
+int eg_load_edges(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int symmetric, int where) {
+    EG_TRY(check_graph(g, "eg_load_edges"));
+    if (edge_bytes != 8 && edge_bytes != 12) {
+        set_error("eg_load_edges: edge_bytes must be 8 ({src,dst}) or 12 ({src,dst,float})");
+        return EG_ERR_INVALID;
+    }
+    if (V == 0) {
+        set_error("eg_load_edges: V must be positive");
+        return EG_ERR_INVALID;
+    }
+    if (E > 0 && !edges) {
+        set_error("eg_load_edges: null edge pointer");
+        return EG_ERR_INVALID;
+    }
+    if (where != EG_HOST && where != EG_DEVICE) {
+        set_error("eg_load_edges: where must be EG_HOST or EG_DEVICE");
+        return EG_ERR_INVALID;
+    }
+    const uint64_t total = symmetric ? 2 * E : E;
+    if (total > (1ull << 40)) {
+        set_error("eg_load_edges: too many edges");
+        return EG_ERR_INVALID;
+    }
+    g->built_csr = g->built_csc = false;
+    g->eng.pull_ready = false;
+    g->V = V;
+    g->E = total;
+    g->edge_bytes = edge_bytes;
+    g->weighted = edge_bytes == 12;
+    g->symmetric = symmetric != 0;
+    EG_TRY(g->edges.reserve((size_t)total * edge_bytes + 64));
+    if (E) {
+        EG_CUDA(cudaMemcpyAsync(g->edges.ptr, edges, (size_t)E * edge_bytes,
+                                where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, g->stream));
+    }
+    EG_TRY(validate_edges(g, E));
+    if (symmetric) EG_TRY(symmetrize_edges(g, E));
+    return EG_OK;
+}
+
+int eg_build(eg_graph* g, int want_csr, int want_csc) {
+    EG_TRY(check_graph(g, "eg_build"));
+    if (g->V == 0) {
+        set_error("eg_build: no edge list loaded");
+        return EG_ERR_STATE;
+    }
+    return build_structures(g, want_csr, want_csc);
+}
+
+int eg_load_directed(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int where) {
+    EG_TRY(eg_load_edges(g, edges, E, V, edge_bytes, 0, where));
+    return eg_build(g, 1, 1);
+}
+
+int eg_load_undirected_from_directed(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes,
+                                     int where) {
+    EG_TRY(eg_load_edges(g, edges, E, V, edge_bytes, 1, where));
+    return eg_build(g, 1, 1);
+}
+
+int eg_get_info(eg_graph* g, eg_info* out) {
+    EG_TRY(check_graph(g, "eg_get_info"));
+    if (!out) {
+        set_error("eg_get_info: null output");
+        return EG_ERR_INVALID;
+    }
+    out->V = g->V;
+    out->partitions = (uint32_t)g->partitions;
+    out->E = g->E;
+    out->ncompressed = g->built_csc ? g->ncompressed : 0;
+    out->weighted = g->weighted;
+    out->built_csr = g->built_csr;
+    out->built_csc = g->built_csc;
+    out->symmetric = g->symmetric;
+    return EG_OK;
+}
+
+int eg_get_partition(eg_graph* g, uint32_t* partition_offset, uint32_t* local_offset) {
+    EG_TRY(check_graph(g, "eg_get_partition"));
+    if (g->part_off.empty()) {
+        set_error("eg_get_partition: graph not built");
+        return EG_ERR_STATE;
+    }
+    if (partition_offset) memcpy(partition_offset, g->part_off.data(), sizeof(uint32_t) * g->part_off.size());
+    if (local_offset) memcpy(local_offset, g->local_off.data(), sizeof(uint32_t) * g->local_off.size());
+    return EG_OK;
+}
+
+int eg_get_degrees(eg_graph* g, uint32_t* outdeg, uint32_t* indeg, int where) {
+    EG_TRY(check_graph(g, "eg_get_degrees"));
+    if (!g->built_csr && !g->built_csc) {
+        set_error("eg_get_degrees: graph not built");
+        return EG_ERR_STATE;
+    }
+    cudaMemcpyKind k = where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (outdeg) EG_CUDA(cudaMemcpyAsync(outdeg, g->outdeg.ptr, sizeof(uint32_t) * (size_t)g->V, k, g->stream));
+    if (indeg) EG_CUDA(cudaMemcpyAsync(indeg, g->indeg.ptr, sizeof(uint32_t) * (size_t)g->V, k, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    return EG_OK;
+}
+
+int eg_get_csr(eg_graph* g, eg_csr_view* out) {
+    EG_TRY(check_graph(g, "eg_get_csr"));
+    if (!out) { set_error("eg_get_csr: null output"); return EG_ERR_INVALID; }
+    if (!g->built_csr) { set_error("eg_get_csr: CSR not built"); return EG_ERR_STATE; }
+    out->off = g->csr_off.as<uint64_t>();
+    out->adj = g->csr_adj.as<uint32_t>();
+    out->w = g->weighted ? g->csr_w.as<float>() : nullptr;
+    out->bitmap = g->csr_bitmap.as<uint64_t>();
+    return EG_OK;
+}
+
+int eg_get_csc(eg_graph* g, eg_csc_view* out) {
+    EG_TRY(check_graph(g, "eg_get_csc"));
+    if (!out) { set_error("eg_get_csc: null output"); return EG_ERR_INVALID; }
+    if (!g->built_csc) { set_error("eg_get_csc: CSC not built"); return EG_ERR_STATE; }
+    out->off = g->csc_off.as<uint64_t>();
+    out->adj = g->csc_adj.as<uint32_t>();
+    out->w = g->weighted ? g->csc_w.as<float>() : nullptr;
+    out->cvert = g->cvert.as<uint32_t>();
+    out->cidx = g->cidx.as<uint64_t>();
+    return EG_OK;
+}
+
+static int copy_dev(eg_graph* g, void* dst, const void* src, size_t bytes, int where) {
+    if (!dst || !bytes) return EG_OK;
+    EG_CUDA(cudaMemcpyAsync(dst, src, bytes, where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                            g->stream));
+    return EG_OK;
+}
+
+int eg_copy_csr(eg_graph* g, uint64_t* off, uint32_t* adj, float* w, uint64_t* bitmap, int where) {
+    EG_TRY(check_graph(g, "eg_copy_csr"));
+    if (!g->built_csr) { set_error("eg_copy_csr: CSR not built"); return EG_ERR_STATE; }
+    const size_t P = (size_t)g->partitions, V = g->V;
+    EG_TRY(copy_dev(g, off, g->csr_off.ptr, sizeof(uint64_t) * P * (V + 1), where));
+    EG_TRY(copy_dev(g, adj, g->csr_adj.ptr, sizeof(uint32_t) * g->E, where));
+    if (g->weighted) EG_TRY(copy_dev(g, w, g->csr_w.ptr, sizeof(float) * g->E, where));
+    EG_TRY(copy_dev(g, bitmap, g->csr_bitmap.ptr, sizeof(uint64_t) * P * (V / 64 + 1), where));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    return EG_OK;
+}
+
+int eg_copy_csc(eg_graph* g, uint64_t* off, uint32_t* adj, float* w, uint32_t* cvert, uint64_t* cidx, int where) {
+    EG_TRY(check_graph(g, "eg_copy_csc"));
+    if (!g->built_csc) { set_error("eg_copy_csc: CSC not built"); return EG_ERR_STATE; }
+    const size_t P = (size_t)g->partitions, V = g->V;
+    EG_TRY(copy_dev(g, off, g->csc_off.ptr, sizeof(uint64_t) * P * (V + 1), where));
+    EG_TRY(copy_dev(g, adj, g->csc_adj.ptr, sizeof(uint32_t) * g->E, where));
+    if (g->weighted) EG_TRY(copy_dev(g, w, g->csc_w.ptr, sizeof(float) * g->E, where));
+    EG_TRY(copy_dev(g, cvert, g->cvert.ptr, sizeof(uint32_t) * g->ncompressed, where));
+    EG_TRY(copy_dev(g, cidx, g->cidx.ptr, sizeof(uint64_t) * g->ncompressed, where));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    return EG_OK;
+}
+
+int eg_cpbt_partition(const uint32_t* deg, uint32_t V, int P, int S, uint64_t eta, int max_iterations, int dense,
+                      int where, uint32_t* partition_offset, uint32_t* local_offset) {
+    if (!deg || !partition_offset || V == 0) {
+        set_error("eg_cpbt_partition: need degrees, output and V > 0");
+        return EG_ERR_INVALID;
+    }
+    eg_graph* raw = nullptr;
+    eg_config cfg = {eta, 1, 1, max_iterations, 0, nullptr};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cfg.device = dev;
+    EG_TRY(eg_create(&raw, &cfg));
+    std::unique_ptr<eg_graph, HandleDeleter> g(raw);
+    const uint32_t* d_deg = deg;
+    DevBuf copy;
+    if (where == EG_HOST) {
+        EG_TRY(copy.reserve(sizeof(uint32_t) * (size_t)V));
+        EG_CUDA(cudaMemcpyAsync(copy.ptr, deg, sizeof(uint32_t) * (size_t)V, cudaMemcpyHostToDevice, g->stream));
+        d_deg = copy.as<uint32_t>();
+    }
+    std::vector<uint32_t> lo((size_t)P * (std::max(S, 1) + 1));
+    EG_TRY(cpbt_device(g.get(), d_deg, V, P, S, eta, max_iterations, dense, partition_offset, lo.data()));
+    if (local_offset) memcpy(local_offset, lo.data(), sizeof(uint32_t) * lo.size());
+    return EG_OK;
+}
+
+int eg_optimal_offset(const uint64_t* a, uint32_t n, uint32_t k, uint32_t* offset) {
+    if ((!a && n) || !offset || k < 1 || k > (uint32_t)kMaxPartitions) {
+        set_error("eg_optimal_offset: need weights, output and 1 <= k <= %d", kMaxPartitions);
+        return EG_ERR_INVALID;
+    }
+    eg_graph* raw = nullptr;
+    eg_config cfg = {1, 1, 1, 1, 0, nullptr};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cfg.device = dev;
+    EG_TRY(eg_create(&raw, &cfg));
+    std::unique_ptr<eg_graph, HandleDeleter> g(raw);
+    DevBuf w;
+    EG_TRY(w.reserve(sizeof(uint64_t) * ((size_t)n + 1)));
+    if (n) EG_CUDA(cudaMemcpyAsync(w.ptr, a, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, g->stream));
+    return cpbt_search(g.get(), w.as<uint64_t>(), n, (int)k, 1, offset, nullptr);
+}
+
+int eg_pagerank(eg_graph* g, int iterations, float damping, float* out, int where) {
+    EG_TRY(check_graph(g, "eg_pagerank"));
+    return run_pagerank(g, iterations, damping, out, where);
+}
+
+int eg_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int where, uint64_t* reached) {
+    EG_TRY(check_graph(g, "eg_bfs"));
+    return run_bfs(g, root, level, parent, where, reached);
+}
+
+int eg_cc(eg_graph* g, uint32_t* label, int where) {
+    EG_TRY(check_graph(g, "eg_cc"));
+    return run_cc(g, label, where);
+}
+
+int eg_sssp(eg_graph* g, uint32_t root, float* dist, int where) {
+    EG_TRY(check_graph(g, "eg_sssp"));
+    return run_sssp(g, root, dist, where);
+}
+
+int eg_last_run(eg_graph* g, uint64_t* edges_processed, int* iterations, int* push_iters, int* pull_iters) {
+    EG_TRY(check_graph(g, "eg_last_run"));
+    if (edges_processed) *edges_processed = g->last_edges_processed;
+    if (iterations) *iterations = g->last_iterations;
+    if (push_iters) *push_iters = g->last_pushes;
+    if (pull_iters) *pull_iters = g->last_pulls;
+    return EG_OK;
+}
+
+int eg_profile_enable(eg_graph* g, int enable) {
+    EG_TRY(check_graph(g, "eg_profile_enable"));
+    g->prof.enabled = enable != 0;
+    return EG_OK;
+}
+
+int eg_profile_reset(eg_graph* g) {
+    EG_TRY(check_graph(g, "eg_profile_reset"));
+    g->prof.clear();
+    return EG_OK;
+}
+
+int eg_profile_read(eg_graph* g, eg_kernel_stat* out, int cap, int* count) {
+    EG_TRY(check_graph(g, "eg_profile_read"));
+    g->prof.collect();
+    int i = 0;
+    for (auto& kv : g->prof.stats) {
+        if (out && i < cap) {
+            memset(out[i].name, 0, sizeof(out[i].name));
+            strncpy(out[i].name, kv.first.c_str(), sizeof(out[i].name) - 1);
+            out[i].launches = kv.second.launches;
+            out[i].ms = kv.second.ms;
+        }
+        ++i;
+    }
+    if (count) *count = i;
+    return EG_OK;
+}
+
+}  // extern "C"

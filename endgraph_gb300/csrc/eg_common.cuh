@@ -1,0 +1,204 @@
+// eg_common.cuh — shared internals of libendgraph_gb300: status handling, device buffers,
+// the graph handle, per-kernel CUDA-event profiling, and small device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/endgraph_gb300.h"
+
+namespace eg {
+
+constexpr uint32_t kPageSize = 4096;  // vertices per CPBT page (core/constants.hpp:21)
+constexpr int kMaxPartitions = 1024;  // virtual partitions on one GPU
+
+// ---------------------------------------------------------------------------------------------
+// status
+void set_error(const char* fmt, ...);
+const char* error_text();
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define EG_CUDA(call)                                                          \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess) return ::eg::cuda_fail(e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define EG_CHECK_LAUNCH(name)                                                  \
+    do {                                                                       \
+        cudaError_t e_ = cudaGetLastError();                                   \
+        if (e_ != cudaSuccess) return ::eg::cuda_fail(e_, name, __FILE__, __LINE__); \
+    } while (0)
+
+#define EG_TRY(expr)                                                           \
+    do {                                                                       \
+        int s_ = (expr);                                                       \
+        if (s_ != EG_OK) return s_;                                            \
+    } while (0)
+
+// ---------------------------------------------------------------------------------------------
+// device memory: one owning buffer type; grows, never shrinks unless released
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    int reserve(size_t n);  // ensure capacity >= n bytes (contents not preserved)
+    void release();
+    template <typename T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+// ---------------------------------------------------------------------------------------------
+// per-kernel timing with CUDA events on the handle's stream
+struct KernelStat {
+    uint64_t launches = 0;
+    double ms = 0;
+};
+
+struct Profiler {
+    bool enabled = false;
+    struct Pending {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> pool;
+    std::map<std::string, KernelStat> stats;
+    cudaEvent_t get();
+    void begin(cudaStream_t s, const char* name);
+    void end(cudaStream_t s);
+    void collect();  // synchronises pending events into stats
+    void clear();
+    ~Profiler();
+};
+
+// RAII launch bracket: records events around a launch when profiling is on
+struct Timed {
+    Profiler* p;
+    cudaStream_t s;
+    Timed(Profiler* prof, cudaStream_t st, const char* name) : p(prof), s(st) {
+        if (p && p->enabled) p->begin(s, name);
+    }
+    ~Timed() {
+        if (p && p->enabled) p->end(s);
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// scan (decoupled look-back) scratch
+struct ScanScratch {
+    DevBuf desc;     // u64 per tile
+    DevBuf counter;  // u32 tile ticket + i32 error flag
+};
+
+// engine scratch
+struct EngineState {
+    DevBuf q0, q1;         // frontier queues (u32 vertex ids)
+    DevBuf qdeg;           // u64 prefix of frontier item degrees
+    DevBuf chunk_item;     // u32 first item per edge chunk
+    DevBuf bm_visit, bm_next;  // bitmaps (u64 words)
+    DevBuf counters;       // u64 small device counters
+    DevBuf acc;            // float / u32 per-vertex accumulator for split items
+    DevBuf vals0, vals1;   // per-vertex values
+    DevBuf pull_chunk_item;  // u32 per CSC chunk: first compressed item
+    DevBuf pull_split;     // u32 list of vertices whose list spans a chunk boundary
+    uint64_t pull_nsplit = 0;
+    uint64_t pull_nchunks = 0;
+    bool pull_ready = false;
+    DevBuf host_pinned_dummy;
+};
+
+}  // namespace eg
+
+// the opaque handle of the C ABI
+struct eg_graph {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // construction parameters (Graph(int eta), toolkit flags)
+    uint64_t eta = 1;
+    int partitions = 1;
+    int sub_partitions = 1;
+    int max_iterations = 20;
+    // loaded edge list
+    uint32_t V = 0;
+    uint64_t E = 0;       // edges after symmetrisation
+    int weighted = 0;
+    int symmetric = 0;
+    eg::DevBuf edges;     // packed records as loaded (8 or 12 bytes each)
+    int edge_bytes = 8;
+    // degrees (u32 V)
+    eg::DevBuf outdeg, indeg;
+    // CPBT
+    std::vector<uint32_t> part_off;   // P+1
+    std::vector<uint32_t> local_off;  // P*(S+1)
+    eg::DevBuf d_part_off;            // P+1 clamped (monotone) copy on device
+    bool built_csr = false, built_csc = false;
+    // partition counts for P > 1 (u32 P*(V+1))
+    eg::DevBuf cnt_csr, cnt_csc;
+    // CSR: P*(V+1) u64 offsets, E u32 dst, E f32 w, P*nwords u64 bitmap
+    eg::DevBuf csr_off, csr_adj, csr_w, csr_bitmap;
+    // CSC: offsets, src, w, compressed (vertex u32, index u64)
+    eg::DevBuf csc_off, csc_adj, csc_w, cvert, cidx;
+    uint64_t ncompressed = 0;
+    std::vector<uint64_t> cstart;  // P+1 entry ranges of the compressed index
+    std::vector<uint64_t> part_edges_csr, part_edges_csc;  // P+1 edge ranges
+    // scratch
+    eg::ScanScratch scan;
+    eg::DevBuf tmp64;  // generic u64 scratch
+    eg::DevBuf cpbt_scratch;
+    eg::DevBuf err;    // device error flags (int)
+    eg::EngineState eng;
+    eg::Profiler prof;
+    // pinned staging for host inputs
+    void* pinned = nullptr;
+    size_t pinned_bytes = 0;
+    // last operator statistics
+    uint64_t last_edges_processed = 0;
+    int last_iterations = 0;
+    int last_pushes = 0, last_pulls = 0;
+};
+
+namespace eg {
+// ---------------------------------------------------------------------------------------------
+// internal entry points shared between translation units
+int scan_u32_to_u64(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out_incl, uint64_t* total_dev);
+int compress_index(eg_graph* g, const uint32_t* cnt, uint64_t n, uint32_t V, const uint64_t* off,
+                   uint32_t* cvert, uint64_t* cidx, uint64_t* count_dev);
+int build_structures(eg_graph* g, int want_csr, int want_csc);
+int compute_degrees(eg_graph* g);
+int cpbt_device(eg_graph* g, const uint32_t* d_deg, uint32_t V, int P, int S, uint64_t eta, int T, int dense,
+                uint32_t* h_part, uint32_t* h_local);
+int cpbt_search(eg_graph* g, const uint64_t* d_w, uint32_t n, int P, int S, uint32_t* po, uint32_t* lpo);
+int check_device_error(eg_graph* g, const char* what);
+int validate_edges(eg_graph* g, uint64_t E);
+int symmetrize_edges(eg_graph* g, uint64_t E);
+int run_pagerank(eg_graph* g, int iterations, float damping, float* out, int where);
+int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int where, uint64_t* reached);
+int run_sssp(eg_graph* g, uint32_t root, float* dist, int where);
+int run_cc(eg_graph* g, uint32_t* label, int where);
+
+// device helpers
+__device__ __forceinline__ uint32_t part_of(const uint32_t* __restrict__ off, int P, uint32_t v) {
+    // off: P+1 clamped monotone offsets; last index i with off[i] <= v (v < off[P] = V)
+    int lo = 0, hi = P;  // answer in [0, P)
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (off[mid] <= v) lo = mid; else hi = mid;
+    }
+    return (uint32_t)lo;
+}
+
+inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap = 152u * 64u) {
+    uint64_t g = (n + block - 1) / block;
+    if (g == 0) g = 1;
+    return (unsigned)(g < cap ? g : cap);
+}
+
+}  // namespace eg

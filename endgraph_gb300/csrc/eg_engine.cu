@@ -1,0 +1,718 @@
+// eg_engine.cu — process_edges on the GPU (core/graph.hpp:1376-1817) for the four toolkits.
+//
+// Push (sparse, :1505-1655): the frontier is a queue of vertices; a look-back scan over the
+// frontier's list lengths gives every frontier edge a global rank, and the expansion kernel hands
+// each CTA a fixed run of 2048 ranks (8 contiguous edges per thread), so hubs and leaves cost the
+// same per edge.  Activations are de-duplicated in a bitmap and appended with warp-aggregated
+// atomics.
+// Pull (dense, :1656-1802): the CSC is swept in fixed 4096-edge chunks (16 contiguous ids per
+// thread, 128-bit loads); a chunk's compressed entries are staged in shared memory and each thread
+// reduces its edges per destination into shared accumulators.  Destinations wholly inside a chunk
+// are finalised in place; the few whose list crosses a chunk boundary are combined afterwards.
+#include <string.h>
+
+#include <algorithm>
+
+#include "eg_common.cuh"
+#include "eg_scan.cuh"
+
+namespace eg {
+
+constexpr int kPullThreads = 256;
+constexpr int kPullPerThread = 16;
+constexpr uint64_t kPullChunk = kPullThreads * kPullPerThread;  // 4096 edges
+constexpr int kPushThreads = 256;
+constexpr int kPushPerThread = 8;
+constexpr uint64_t kPushChunk = kPushThreads * kPushPerThread;  // 2048 edges
+constexpr unsigned kPersistentGrid = 152u * 8u;
+
+// ---------------------------------------------------------------------------------------------
+// pull setup: chunk -> first compressed item, and the list of destinations split across chunks
+__global__ void k_pull_chunks(const uint64_t* __restrict__ cidx, const uint32_t* __restrict__ cvert, uint64_t nitems,
+                              uint64_t nchunks, uint32_t* __restrict__ chunk_item, uint32_t* __restrict__ split,
+                              unsigned long long* nsplit) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nitems; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t s = cidx[i], e = cidx[i + 1];
+        if (e <= s) continue;
+        uint64_t c0 = (s + kPullChunk - 1) / kPullChunk, c1 = (e + kPullChunk - 1) / kPullChunk;
+        for (uint64_t c = c0; c < c1; ++c) chunk_item[c] = (uint32_t)i;
+        if (s / kPullChunk != (e - 1) / kPullChunk && cvert[i] != 0xFFFFFFFFu) {
+            unsigned long long k = atomicAdd(nsplit, 1ull);
+            split[k] = (uint32_t)i;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) chunk_item[nchunks] = (uint32_t)nitems;
+}
+
+// Generic segmented pull over compressed CSC entries.  Op provides:
+//   Acc identity(); Acc gather(uint32_t src, uint64_t epos); Acc combine(Acc, Acc);
+//   void smem_add(Acc* slot, Acc v); void finish(uint32_t v, Acc a, bool whole)
+template <class Op>
+__global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __restrict__ adj,
+                                                        const uint64_t* __restrict__ cidx,
+                                                        const uint32_t* __restrict__ cvert,
+                                                        const uint32_t* __restrict__ chunk_item, uint64_t E,
+                                                        uint64_t nitems, uint64_t nchunks, uint32_t V) {
+    using Acc = typename Op::Acc;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const int cap = (int)kPullChunk + kMaxPartitions + 2;
+    uint64_t* s_idx = reinterpret_cast<uint64_t*>(s_raw);
+    Acc* s_acc = reinterpret_cast<Acc*>(s_idx + cap + 1);
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint64_t e0 = c * kPullChunk;
+        const uint64_t e1 = e0 + kPullChunk < E ? e0 + kPullChunk : E;
+        const uint32_t i0 = chunk_item[c];
+        const uint32_t j = chunk_item[c + 1];
+        const uint32_t iend = (j < nitems && cidx[j] < e1) ? j + 1 : j;
+        const int nit = (int)(iend - i0);
+        for (int k = threadIdx.x; k <= nit; k += blockDim.x) {
+            s_idx[k] = cidx[i0 + k];
+            if (k < nit) s_acc[k] = op.identity();
+        }
+        __syncthreads();
+        const uint64_t eb = e0 + (uint64_t)threadIdx.x * kPullPerThread;
+        if (eb < e1) {
+            const uint64_t ee = eb + kPullPerThread < e1 ? eb + kPullPerThread : e1;
+            uint32_t ids[kPullPerThread];
+            if (ee - eb == kPullPerThread) {
+                const uint4* p = reinterpret_cast<const uint4*>(adj + eb);
+#pragma unroll
+                for (int q = 0; q < kPullPerThread / 4; ++q) {
+                    uint4 x = __ldcs(p + q);
+                    ids[4 * q] = x.x; ids[4 * q + 1] = x.y; ids[4 * q + 2] = x.z; ids[4 * q + 3] = x.w;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < kPullPerThread; ++q) ids[q] = eb + q < ee ? adj[eb + q] : 0u;
+            }
+            Acc vals[kPullPerThread];
+#pragma unroll
+            for (int q = 0; q < kPullPerThread; ++q) vals[q] = eb + q < ee ? op.gather(ids[q], eb + q) : op.identity();
+            // item holding eb: last k with s_idx[k] <= eb
+            int lo = 0, hi = nit;
+            while (hi - lo > 1) {
+                int mid = (lo + hi) >> 1;
+                if (s_idx[mid] <= eb) lo = mid; else hi = mid;
+            }
+            int k = lo;
+            uint64_t nb = s_idx[k + 1];
+            Acc a = op.identity();
+#pragma unroll
+            for (int q = 0; q < kPullPerThread; ++q) {
+                const uint64_t e = eb + q;
+                if (e < ee) {
+                    while (e >= nb) {
+                        op.smem_add(&s_acc[k], a);
+                        a = op.identity();
+                        ++k;
+                        nb = s_idx[k + 1];
+                    }
+                    a = op.combine(a, vals[q]);
+                }
+            }
+            op.smem_add(&s_acc[k], a);
+        }
+        __syncthreads();
+        const int rounds = (nit + (int)blockDim.x - 1) / (int)blockDim.x;
+        for (int r = 0; r < rounds; ++r) {
+            int k = r * blockDim.x + threadIdx.x;
+            bool ok = k < nit;
+            uint32_t v = ok ? cvert[i0 + k] : V;
+            if (v >= V) ok = false;  // partition sentinels
+            Acc a = ok ? s_acc[k] : op.identity();
+            bool whole = ok && s_idx[k] >= e0 && s_idx[k + 1] <= e1;
+            op.finish(ok, v, a, whole);
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// warp-aggregated append of activated vertices to a queue
+__device__ __forceinline__ void append_active(bool act, uint32_t w, uint32_t* q_out, uint32_t* n_out,
+                                              unsigned long long* act_edges, const uint32_t* deg) {
+    const unsigned mask = __ballot_sync(0xffffffffu, act);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(n_out, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (act) {
+        q_out[base + __popc(mask & ((1u << lane) - 1u))] = w;
+        if (act_edges) atomicAdd(act_edges, (unsigned long long)deg[w]);
+    }
+}
+
+// push expansion over the frontier items (vertex q[i / P], partition i % P)
+struct PushArgs {
+    const uint32_t* q;
+    uint64_t nitems;
+    int P;
+    uint64_t stride;
+    const uint64_t* off;
+    const uint32_t* adj;
+    const float* w;
+    const uint64_t* ipref;  // exclusive prefix of item lengths, ipref[nitems] = total
+    const uint32_t* chunk_item;
+    uint32_t* q_out;
+    uint32_t* n_out;
+    unsigned long long* act_edges;
+    const uint32_t* deg;
+};
+
+template <class Op>
+__global__ void __launch_bounds__(kPushThreads) k_push(Op op, PushArgs a) {
+    const uint64_t T = a.ipref[a.nitems];
+    const uint64_t nchunks = (T + kPushChunk - 1) / kPushChunk;
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint64_t e0 = c * kPushChunk;
+        const uint64_t e1 = e0 + kPushChunk < T ? e0 + kPushChunk : T;
+        const uint64_t eb = e0 + (uint64_t)threadIdx.x * kPushPerThread;
+        const uint64_t ee = eb + kPushPerThread < e1 ? eb + kPushPerThread : e1;
+        // item holding rank eb: last i in [i0, i1] with ipref[i] <= eb
+        uint64_t lo = a.chunk_item[c];
+        uint64_t hi = (c + 1 < nchunks) ? (uint64_t)a.chunk_item[c + 1] + 1 : a.nitems;
+        if (eb < ee) {
+            while (hi - lo > 1) {
+                uint64_t mid = (lo + hi) >> 1;
+                if (a.ipref[mid] <= eb) lo = mid; else hi = mid;
+            }
+        }
+        uint64_t it = lo;
+        uint64_t ibeg = a.ipref[it], iend = a.ipref[it + 1];
+        uint32_t u = a.q[it / a.P];
+        uint64_t lbase = a.off[(it % a.P) * a.stride + u];
+        uint32_t pay = op.payload(u);
+#pragma unroll
+        for (int q = 0; q < kPushPerThread; ++q) {
+            const uint64_t e = eb + q;
+            bool act = false;
+            uint32_t wv = 0;
+            if (e < ee) {
+                while (e >= iend) {
+                    ++it;
+                    ibeg = iend;
+                    iend = a.ipref[it + 1];
+                    u = a.q[it / a.P];
+                    lbase = a.off[(it % a.P) * a.stride + u];
+                    pay = op.payload(u);
+                }
+                const uint64_t pos = lbase + (e - ibeg);
+                wv = a.adj[pos];
+                act = op.relax(u, pay, wv, pos);
+            }
+            append_active(act, wv, a.q_out, a.n_out, a.act_edges, a.deg);
+        }
+    }
+}
+
+// scan over frontier items: item length -> exclusive rank, and chunk -> first item
+struct LoadItemLen {
+    const uint32_t* q;
+    int P;
+    uint64_t stride;
+    const uint64_t* off;
+    __device__ uint32_t operator()(uint64_t i) const {
+        uint32_t u = q[i / P];
+        uint64_t b = (i % P) * stride + u;
+        return (uint32_t)(off[b + 1] - off[b]);
+    }
+};
+struct EpiItemRank {
+    uint64_t* ipref;
+    uint32_t* chunk_item;
+    __device__ void operator()(uint64_t i, uint64_t excl, uint32_t len) const {
+        ipref[i] = excl;
+        uint64_t c0 = (excl + kPushChunk - 1) / kPushChunk, c1 = (excl + len + kPushChunk - 1) / kPushChunk;
+        for (uint64_t c = c0; c < c1; ++c) chunk_item[c] = (uint32_t)i;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// toolkit operators
+struct BfsOp {  // toolkits/bfs.cpp:52-58: first visitor of dst becomes its parent
+    unsigned long long* visited;
+    uint32_t* level;
+    uint32_t* parent;
+    uint32_t next_level;
+    __device__ uint32_t payload(uint32_t) const { return 0; }
+    __device__ bool relax(uint32_t u, uint32_t, uint32_t w, uint64_t) const {
+        const unsigned long long bit = 1ull << (w & 63);
+        unsigned long long* word = visited + (w >> 6);
+        if (__ldcg(word) & bit) return false;
+        if (atomicOr(word, bit) & bit) return false;
+        if (level) level[w] = next_level;
+        if (parent) parent[w] = u;
+        return true;
+    }
+};
+
+struct SsspOp {  // toolkits/sssp.cpp:52-64: relax_dist = dist[src] + w; write_min
+    float* dist;
+    const float* wts;
+    unsigned long long* next_bm;
+    __device__ uint32_t payload(uint32_t u) const { return __float_as_uint(__ldcg(dist + u)); }
+    __device__ bool relax(uint32_t, uint32_t pay, uint32_t w, uint64_t pos) const {
+        const float nd = __uint_as_float(pay) + wts[pos];
+        if (!(nd < __ldcg(dist + w))) return false;
+        const int old = atomicMin(reinterpret_cast<int*>(dist + w), __float_as_int(nd));
+        if (!(nd < __int_as_float(old))) return false;
+        const unsigned long long bit = 1ull << (w & 63);
+        return !(atomicOr(next_bm + (w >> 6), bit) & bit);
+    }
+};
+
+struct CcPushOp {  // toolkits/cc.cpp:50-60: msg = label[src]; write_min(label[dst], msg)
+    uint32_t* label;
+    unsigned long long* next_bm;
+    __device__ uint32_t payload(uint32_t u) const { return __ldcg(label + u); }
+    __device__ bool relax(uint32_t, uint32_t pay, uint32_t w, uint64_t) const {
+        if (!(pay < __ldcg(label + w))) return false;
+        const uint32_t old = atomicMin(label + w, pay);
+        if (!(pay < old)) return false;
+        const unsigned long long bit = 1ull << (w & 63);
+        return !(atomicOr(next_bm + (w >> 6), bit) & bit);
+    }
+};
+
+struct PrPullOp {  // toolkits/pagerank.cpp:64-97: sum curr[src]; next = 1-d+d*sum (/ outdeg)
+    using Acc = float;
+    const float* curr;
+    float* next;
+    float* acc;
+    const uint32_t* outdeg;
+    float base, d;
+    int divide, single;
+    __device__ Acc identity() const { return 0.f; }
+    __device__ Acc gather(uint32_t src, uint64_t) const { return __ldg(curr + src); }
+    __device__ Acc combine(Acc a, Acc b) const { return a + b; }
+    __device__ void smem_add(Acc* slot, Acc v) const { atomicAdd(slot, v); }
+    __device__ void finish(bool ok, uint32_t v, Acc a, bool whole) const {
+        if (!ok) return;
+        if (whole && single) {
+            float x = base + d * a;
+            if (divide) {
+                uint32_t dg = outdeg[v];
+                if (dg > 0) x /= (float)dg;
+            }
+            next[v] = x;
+        } else {
+            atomicAdd(acc + v, a);
+        }
+    }
+};
+
+struct CcPullOp {  // toolkits/cc.cpp:62-80: min label over in-neighbours, write_min + activate
+    using Acc = uint32_t;
+    uint32_t* label;
+    unsigned long long* next_bm;
+    uint32_t* q_out;
+    uint32_t* n_out;
+    unsigned long long* act_edges;
+    const uint32_t* deg;
+    __device__ Acc identity() const { return 0xFFFFFFFFu; }
+    __device__ Acc gather(uint32_t src, uint64_t) const { return __ldcg(label + src); }
+    __device__ Acc combine(Acc a, Acc b) const { return a < b ? a : b; }
+    __device__ void smem_add(Acc* slot, Acc v) const { atomicMin(slot, v); }
+    __device__ void finish(bool ok, uint32_t v, Acc m, bool) const {
+        bool act = false;
+        if (ok && m < __ldcg(label + v)) {
+            uint32_t old = atomicMin(label + v, m);
+            if (m < old) {
+                const unsigned long long bit = 1ull << (v & 63);
+                act = !(atomicOr(next_bm + (v >> 6), bit) & bit);
+            }
+        }
+        append_active(act, v, q_out, n_out, act_edges, deg);
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// vertex passes
+__global__ void k_fill_u32(uint32_t* p, uint64_t n, uint32_t v) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+__global__ void k_fill_f32(float* p, uint64_t n, float v) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+__global__ void k_iota(uint32_t* p, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) p[i] = (uint32_t)i;
+}
+__global__ void k_pr_init(float* curr, const uint32_t* __restrict__ outdeg, uint32_t V) {  // pagerank.cpp:36-45
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t dg = outdeg[v];
+        curr[v] = dg > 0 ? 1.0f / (float)dg : 1.0f;
+    }
+}
+// vertices without in-edges: next = 1-d (/ outdeg)
+__global__ void k_pr_zero_in(float* buf, const uint32_t* __restrict__ indeg, const uint32_t* __restrict__ outdeg,
+                             uint32_t V, float base, int divide) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x) {
+        if (indeg[v] == 0) {
+            uint32_t dg = outdeg[v];
+            buf[v] = (divide && dg > 0) ? base / (float)dg : base;
+        }
+    }
+}
+// destinations whose list crossed a chunk boundary (P == 1)
+__global__ void k_pr_split(const uint32_t* __restrict__ split, const uint32_t* __restrict__ cvert, uint64_t nsplit,
+                           float* next, float* acc, const uint32_t* __restrict__ outdeg, float base, float d, int divide) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nsplit; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t v = cvert[split[i]];
+        float x = base + d * acc[v];
+        acc[v] = 0.f;
+        if (divide) {
+            uint32_t dg = outdeg[v];
+            if (dg > 0) x /= (float)dg;
+        }
+        next[v] = x;
+    }
+}
+// P > 1: every destination with in-edges combines its partial sums
+__global__ void k_pr_finish_all(const uint32_t* __restrict__ indeg, uint32_t V, float* next, float* acc,
+                                const uint32_t* __restrict__ outdeg, float base, float d, int divide) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x) {
+        if (indeg[v] == 0) continue;
+        float x = base + d * acc[v];
+        acc[v] = 0.f;
+        if (divide) {
+            uint32_t dg = outdeg[v];
+            if (dg > 0) x /= (float)dg;
+        }
+        next[v] = x;
+    }
+}
+__global__ void k_bfs_root(uint32_t* level, uint32_t* parent, unsigned long long* visited, uint32_t root, uint32_t* q) {
+    if (level) level[root] = 0;
+    if (parent) parent[root] = root;
+    visited[root >> 6] |= 1ull << (root & 63);
+    q[0] = root;
+}
+__global__ void k_sssp_root(float* dist, uint32_t root, uint32_t* q) {
+    dist[root] = 0.f;
+    q[0] = root;
+}
+
+// ---------------------------------------------------------------------------------------------
+static int setup_pull(eg_graph* g) {
+    EngineState& s = g->eng;
+    if (s.pull_ready) return EG_OK;
+    const uint64_t nitems = g->ncompressed - 1;  // the last sentinel closes the final item
+    const uint64_t nchunks = (g->E + kPullChunk - 1) / kPullChunk;
+    EG_TRY(s.pull_chunk_item.reserve(sizeof(uint32_t) * (nchunks + 2)));
+    EG_TRY(s.pull_split.reserve(sizeof(uint32_t) * (nchunks + 2)));
+    EG_TRY(s.counters.reserve(64));
+    unsigned long long* nsplit = s.counters.as<unsigned long long>();
+    EG_CUDA(cudaMemsetAsync(nsplit, 0, 8, g->stream));
+    // mark sentinels so they never join the split list (their cvert is V, which is not a vertex)
+    {
+        Timed t(&g->prof, g->stream, "pull_setup");
+        k_pull_chunks<<<grid_for(nitems, 256), 256, 0, g->stream>>>(g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(), nitems,
+                                                                    nchunks, s.pull_chunk_item.as<uint32_t>(),
+                                                                    s.pull_split.as<uint32_t>(), nsplit);
+        EG_CHECK_LAUNCH("k_pull_chunks");
+    }
+    unsigned long long h = 0;
+    EG_CUDA(cudaMemcpyAsync(&h, nsplit, 8, cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    s.pull_nsplit = h;
+    s.pull_nchunks = nchunks;
+    s.pull_ready = true;
+    return EG_OK;
+}
+
+template <class Op>
+static int launch_pull(eg_graph* g, const Op& op, const char* name) {
+    EngineState& s = g->eng;
+    const uint64_t nitems = g->ncompressed - 1;
+    if (s.pull_nchunks == 0) return EG_OK;
+    const size_t cap = kPullChunk + kMaxPartitions + 2;
+    const size_t smem = sizeof(uint64_t) * (cap + 1) + sizeof(typename Op::Acc) * cap;
+    EG_CUDA(cudaFuncSetAttribute(k_pull<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    unsigned grid = (unsigned)std::min<uint64_t>(s.pull_nchunks, 152ull * 4ull);
+    Timed t(&g->prof, g->stream, name);
+    k_pull<Op><<<grid, kPullThreads, smem, g->stream>>>(op, g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(),
+                                                        g->cvert.as<uint32_t>(), s.pull_chunk_item.as<uint32_t>(), g->E,
+                                                        nitems, s.pull_nchunks, g->V);
+    EG_CHECK_LAUNCH(name);
+    return EG_OK;
+}
+
+static int ensure_engine(eg_graph* g) {
+    EngineState& s = g->eng;
+    const uint64_t V = g->V;
+    const uint64_t nitems_max = V * (uint64_t)g->partitions + 1;
+    EG_TRY(s.q0.reserve(sizeof(uint32_t) * (V + 1)));
+    EG_TRY(s.q1.reserve(sizeof(uint32_t) * (V + 1)));
+    EG_TRY(s.qdeg.reserve(sizeof(uint64_t) * (nitems_max + 1)));
+    EG_TRY(s.chunk_item.reserve(sizeof(uint32_t) * (g->E / kPushChunk + 4)));
+    EG_TRY(s.bm_visit.reserve(sizeof(uint64_t) * (V / 64 + 1)));
+    EG_TRY(s.bm_next.reserve(sizeof(uint64_t) * (V / 64 + 1)));
+    EG_TRY(s.counters.reserve(64));
+    EG_TRY(s.acc.reserve(sizeof(float) * (V + 1)));
+    EG_TRY(s.vals0.reserve(sizeof(float) * (V + 1)));
+    EG_TRY(s.vals1.reserve(sizeof(float) * (V + 1)));
+    return EG_OK;
+}
+
+// one push level over queue `q` of n vertices; returns the new queue length via *n_out_host
+template <class Op>
+static int push_level(eg_graph* g, const Op& op, uint32_t* q, uint64_t n, uint32_t* q_out, uint32_t* n_out_host,
+                      uint64_t* edges_host, unsigned long long* act_edges_host, const uint32_t* act_deg,
+                      const char* name) {
+    EngineState& s = g->eng;
+    const int P = g->partitions;
+    const uint64_t nitems = n * (uint64_t)P;
+    uint64_t* ipref = s.qdeg.as<uint64_t>();
+    uint32_t* d_nout = reinterpret_cast<uint32_t*>(s.counters.as<unsigned long long>() + 2);
+    unsigned long long* d_act = s.counters.as<unsigned long long>() + 3;
+    EG_CUDA(cudaMemsetAsync(s.counters.as<unsigned long long>() + 2, 0, 16, g->stream));
+    LoadItemLen ld{q, P, (uint64_t)g->V + 1, g->csr_off.as<uint64_t>()};
+    EpiItemRank ep{ipref, s.chunk_item.as<uint32_t>()};
+    EG_TRY(launch_scan(g, ld, ep, nitems, ipref + nitems, "push_rank"));
+    PushArgs a;
+    a.q = q;
+    a.nitems = nitems;
+    a.P = P;
+    a.stride = (uint64_t)g->V + 1;
+    a.off = g->csr_off.as<uint64_t>();
+    a.adj = g->csr_adj.as<uint32_t>();
+    a.w = g->csr_w.as<float>();
+    a.ipref = ipref;
+    a.chunk_item = s.chunk_item.as<uint32_t>();
+    a.q_out = q_out;
+    a.n_out = d_nout;
+    a.act_edges = act_deg ? d_act : nullptr;
+    a.deg = act_deg;
+    {
+        Timed t(&g->prof, g->stream, name);
+        k_push<Op><<<kPersistentGrid, kPushThreads, 0, g->stream>>>(op, a);
+        EG_CHECK_LAUNCH(name);
+    }
+    struct {
+        uint32_t n;
+        uint32_t pad;
+        unsigned long long act;
+    } h;
+    uint64_t T = 0;
+    EG_CUDA(cudaMemcpyAsync(&h, d_nout, 16, cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaMemcpyAsync(&T, ipref + nitems, 8, cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    *n_out_host = h.n;
+    if (edges_host) *edges_host = T;
+    if (act_edges_host) *act_edges_host = h.act;
+    return EG_OK;
+}
+
+static int copy_out(eg_graph* g, void* dst, const void* src, size_t bytes, int where) {
+    if (!dst) return EG_OK;
+    EG_CUDA(cudaMemcpyAsync(dst, src, bytes, where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                            g->stream));
+    return EG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+int run_pagerank(eg_graph* g, int iterations, float damping, float* out, int where) {
+    if (!g->built_csc) { set_error("eg_pagerank: CSC not built"); return EG_ERR_STATE; }
+    if (iterations < 0) { set_error("eg_pagerank: iterations must be >= 0"); return EG_ERR_INVALID; }
+    EG_TRY(ensure_engine(g));
+    EG_TRY(setup_pull(g));
+    const uint32_t V = g->V;
+    EngineState& s = g->eng;
+    float* A = s.vals0.as<float>();
+    float* B = s.vals1.as<float>();
+    const float base = 1.0f - damping;
+    const int single = g->partitions == 1;
+    const unsigned gv = grid_for(V, 256, 152u * 16u);
+    {
+        Timed t(&g->prof, g->stream, "pr_vertex");
+        k_pr_init<<<gv, 256, 0, g->stream>>>(A, g->outdeg.as<uint32_t>(), V);
+        EG_CHECK_LAUNCH("k_pr_init");
+        EG_CUDA(cudaMemsetAsync(s.acc.ptr, 0, sizeof(float) * (size_t)V, g->stream));
+    }
+    for (int it = 0; it < iterations; ++it) {
+        const int last = it == iterations - 1;
+        float* curr = (it & 1) ? B : A;
+        float* next = (it & 1) ? A : B;
+        if (it < 2 || last) {
+            Timed t(&g->prof, g->stream, "pr_vertex");
+            k_pr_zero_in<<<gv, 256, 0, g->stream>>>(next, g->indeg.as<uint32_t>(), g->outdeg.as<uint32_t>(), V, base, !last);
+            EG_CHECK_LAUNCH("k_pr_zero_in");
+        }
+        PrPullOp op{curr, next, s.acc.as<float>(), g->outdeg.as<uint32_t>(), base, damping, !last, single};
+        EG_TRY(launch_pull(g, op, "pr_pull"));
+        Timed t(&g->prof, g->stream, "pr_finish");
+        if (single) {
+            if (s.pull_nsplit) {
+                k_pr_split<<<grid_for(s.pull_nsplit, 256), 256, 0, g->stream>>>(
+                    s.pull_split.as<uint32_t>(), g->cvert.as<uint32_t>(), s.pull_nsplit, next, s.acc.as<float>(),
+                    g->outdeg.as<uint32_t>(), base, damping, !last);
+                EG_CHECK_LAUNCH("k_pr_split");
+            }
+        } else {
+            k_pr_finish_all<<<gv, 256, 0, g->stream>>>(g->indeg.as<uint32_t>(), V, next, s.acc.as<float>(),
+                                                       g->outdeg.as<uint32_t>(), base, damping, !last);
+            EG_CHECK_LAUNCH("k_pr_finish_all");
+        }
+    }
+    float* result = (iterations & 1) ? B : A;
+    EG_TRY(copy_out(g, out, result, sizeof(float) * (size_t)V, where));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    g->last_edges_processed = g->E * (uint64_t)iterations;
+    g->last_iterations = iterations;
+    g->last_pushes = 0;
+    g->last_pulls = iterations;
+    return EG_OK;
+}
+
+int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int where, uint64_t* reached) {
+    if (!g->built_csr) { set_error("eg_bfs: CSR not built"); return EG_ERR_STATE; }
+    if (root >= g->V) { set_error("eg_bfs: root %u >= V %u", root, g->V); return EG_ERR_INVALID; }
+    EG_TRY(ensure_engine(g));
+    const uint32_t V = g->V;
+    EngineState& s = g->eng;
+    uint32_t* d_level = s.vals0.as<uint32_t>();
+    uint32_t* d_parent = s.vals1.as<uint32_t>();
+    const unsigned gv = grid_for(V, 256, 152u * 16u);
+    {
+        Timed t(&g->prof, g->stream, "bfs_init");
+        k_fill_u32<<<gv, 256, 0, g->stream>>>(d_level, V, 0xFFFFFFFFu);
+        k_fill_u32<<<gv, 256, 0, g->stream>>>(d_parent, V, V);
+        EG_CUDA(cudaMemsetAsync(s.bm_visit.ptr, 0, sizeof(uint64_t) * (V / 64 + 1), g->stream));
+        k_bfs_root<<<1, 1, 0, g->stream>>>(d_level, d_parent, s.bm_visit.as<unsigned long long>(), root, s.q0.as<uint32_t>());
+        EG_CHECK_LAUNCH("k_bfs_root");
+    }
+    uint32_t* qa = s.q0.as<uint32_t>();
+    uint32_t* qb = s.q1.as<uint32_t>();
+    uint64_t n = 1, total_edges = 0, reach = 1;
+    uint32_t lvl = 0;
+    while (n > 0) {
+        BfsOp op{s.bm_visit.as<unsigned long long>(), d_level, d_parent, lvl + 1};
+        uint32_t nout = 0;
+        uint64_t T = 0;
+        EG_TRY(push_level(g, op, qa, n, qb, &nout, &T, nullptr, nullptr, "bfs_push"));
+        total_edges += T;
+        reach += nout;
+        std::swap(qa, qb);
+        n = nout;
+        ++lvl;
+    }
+    EG_TRY(copy_out(g, level, d_level, sizeof(uint32_t) * (size_t)V, where));
+    EG_TRY(copy_out(g, parent, d_parent, sizeof(uint32_t) * (size_t)V, where));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    if (reached) *reached = reach;
+    g->last_edges_processed = total_edges;
+    g->last_iterations = (int)lvl;
+    g->last_pushes = (int)lvl;
+    g->last_pulls = 0;
+    return EG_OK;
+}
+
+int run_sssp(eg_graph* g, uint32_t root, float* dist, int where) {
+    if (!g->built_csr) { set_error("eg_sssp: CSR not built"); return EG_ERR_STATE; }
+    if (!g->weighted) { set_error("eg_sssp: graph has no edge weights (load 12-byte records)"); return EG_ERR_STATE; }
+    if (root >= g->V) { set_error("eg_sssp: root %u >= V %u", root, g->V); return EG_ERR_INVALID; }
+    EG_TRY(ensure_engine(g));
+    const uint32_t V = g->V;
+    EngineState& s = g->eng;
+    float* d_dist = s.vals0.as<float>();
+    const size_t bm_bytes = sizeof(uint64_t) * (V / 64 + 1);
+    {
+        Timed t(&g->prof, g->stream, "sssp_init");
+        k_fill_f32<<<grid_for(V, 256, 152u * 16u), 256, 0, g->stream>>>(d_dist, V, 1e9f);
+        EG_CUDA(cudaMemsetAsync(s.bm_next.ptr, 0, bm_bytes, g->stream));
+        k_sssp_root<<<1, 1, 0, g->stream>>>(d_dist, root, s.q0.as<uint32_t>());
+        EG_CHECK_LAUNCH("k_sssp_root");
+    }
+    uint32_t* qa = s.q0.as<uint32_t>();
+    uint32_t* qb = s.q1.as<uint32_t>();
+    uint64_t n = 1, total_edges = 0;
+    int iters = 0;
+    while (n > 0) {
+        SsspOp op{d_dist, g->csr_w.as<float>(), s.bm_next.as<unsigned long long>()};
+        uint32_t nout = 0;
+        uint64_t T = 0;
+        EG_TRY(push_level(g, op, qa, n, qb, &nout, &T, nullptr, nullptr, "sssp_push"));
+        EG_CUDA(cudaMemsetAsync(s.bm_next.ptr, 0, bm_bytes, g->stream));
+        total_edges += T;
+        std::swap(qa, qb);
+        n = nout;
+        ++iters;
+    }
+    EG_TRY(copy_out(g, dist, d_dist, sizeof(float) * (size_t)V, where));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    g->last_edges_processed = total_edges;
+    g->last_iterations = iters;
+    g->last_pushes = iters;
+    g->last_pulls = 0;
+    return EG_OK;
+}
+
+int run_cc(eg_graph* g, uint32_t* label, int where) {
+    if (!g->built_csr || !g->built_csc) { set_error("eg_cc: CSR and CSC must be built"); return EG_ERR_STATE; }
+    EG_TRY(ensure_engine(g));
+    EG_TRY(setup_pull(g));
+    const uint32_t V = g->V;
+    EngineState& s = g->eng;
+    uint32_t* d_label = s.vals0.as<uint32_t>();
+    const size_t bm_bytes = sizeof(uint64_t) * (V / 64 + 1);
+    const unsigned gv = grid_for(V, 256, 152u * 16u);
+    uint32_t* qa = s.q0.as<uint32_t>();
+    uint32_t* qb = s.q1.as<uint32_t>();
+    {
+        Timed t(&g->prof, g->stream, "cc_init");
+        k_iota<<<gv, 256, 0, g->stream>>>(d_label, V);  // cc.cpp:31-37
+        k_iota<<<gv, 256, 0, g->stream>>>(qa, V);       // active_in->fill()
+        EG_CHECK_LAUNCH("k_iota");
+        EG_CUDA(cudaMemsetAsync(s.bm_next.ptr, 0, bm_bytes, g->stream));
+    }
+    uint64_t n = V;
+    unsigned long long active_edges = g->E;  // every vertex active: sum of out-degrees
+    uint64_t total_edges = 0;
+    int iters = 0, pushes = 0, pulls = 0;
+    uint32_t* d_nout = reinterpret_cast<uint32_t*>(s.counters.as<unsigned long long>() + 2);
+    unsigned long long* d_act = s.counters.as<unsigned long long>() + 3;
+    while (n > 0) {
+        uint32_t nout = 0;
+        unsigned long long act = 0;
+        // core/graph.hpp:1484-1491: sparse iff active_edges < edges / 20
+        const bool sparse = active_edges < g->E / 20;
+        if (sparse) {
+            CcPushOp op{d_label, s.bm_next.as<unsigned long long>()};
+            uint64_t T = 0;
+            EG_TRY(push_level(g, op, qa, n, qb, &nout, &T, &act, g->outdeg.as<uint32_t>(), "cc_push"));
+            total_edges += T;
+            ++pushes;
+        } else {
+            EG_CUDA(cudaMemsetAsync(s.counters.as<unsigned long long>() + 2, 0, 16, g->stream));
+            CcPullOp op{d_label, s.bm_next.as<unsigned long long>(), qb, d_nout, d_act, g->outdeg.as<uint32_t>()};
+            EG_TRY(launch_pull(g, op, "cc_pull"));
+            struct {
+                uint32_t n;
+                uint32_t pad;
+                unsigned long long act;
+            } h;
+            EG_CUDA(cudaMemcpyAsync(&h, d_nout, 16, cudaMemcpyDeviceToHost, g->stream));
+            EG_CUDA(cudaStreamSynchronize(g->stream));
+            nout = h.n;
+            act = h.act;
+            total_edges += g->E;
+            ++pulls;
+        }
+        EG_CUDA(cudaMemsetAsync(s.bm_next.ptr, 0, bm_bytes, g->stream));
+        std::swap(qa, qb);
+        n = nout;
+        active_edges = act;
+        ++iters;
+    }
+    EG_TRY(copy_out(g, label, d_label, sizeof(uint32_t) * (size_t)V, where));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    g->last_edges_processed = total_edges;
+    g->last_iterations = iters;
+    g->last_pushes = pushes;
+    g->last_pulls = pulls;
+    return EG_OK;
+}
+
+}  // namespace eg

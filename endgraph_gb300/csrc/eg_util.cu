@@ -1,0 +1,194 @@
+// eg_util.cu — status messages, device buffers, CUDA-event profiler, the R-MAT generator kernel.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "../../include/endgraph_rmat.h"
+#include "eg_common.cuh"
+#include "eg_scan.cuh"
+
+namespace eg {
+
+static thread_local char t_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_err, sizeof(t_err), fmt, ap);
+    va_end(ap);
+}
+
+const char* error_text() { return t_err; }
+
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    set_error("%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    return e == cudaErrorMemoryAllocation ? EG_ERR_NOMEM : EG_ERR_CUDA;
+}
+
+int DevBuf::reserve(size_t n) {
+    if (n <= bytes && ptr) return EG_OK;
+    release();
+    size_t want = n ? n : 16;
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        bytes = 0;
+        cudaGetLastError();
+        set_error("device allocation of %zu bytes failed: %s", want, cudaGetErrorString(e));
+        return EG_ERR_NOMEM;
+    }
+    bytes = want;
+    return EG_OK;
+}
+
+void DevBuf::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+cudaEvent_t Profiler::get() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void Profiler::begin(cudaStream_t s, const char* name) {
+    Pending p;
+    p.name = name;
+    p.a = get();
+    p.b = get();
+    cudaEventRecord(p.a, s);
+    pending.push_back(p);
+}
+
+void Profiler::end(cudaStream_t s) {
+    if (!pending.empty()) cudaEventRecord(pending.back().b, s);
+}
+
+void Profiler::collect() {
+    for (auto& p : pending) {
+        cudaEventSynchronize(p.b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        KernelStat& k = stats[p.name];
+        k.launches += 1;
+        k.ms += ms;
+        pool.push_back(p.a);
+        pool.push_back(p.b);
+    }
+    pending.clear();
+}
+
+void Profiler::clear() {
+    collect();
+    stats.clear();
+}
+
+Profiler::~Profiler() {
+    for (auto& p : pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (auto e : pool) cudaEventDestroy(e);
+}
+
+int check_device_error(eg_graph* g, const char* what) {
+    int h = 0;
+    EG_CUDA(cudaMemcpyAsync(&h, g->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    if (h) {
+        cudaMemsetAsync(g->err.ptr, 0, sizeof(int), g->stream);
+        set_error("%s: a bounded device wait gave up (code %d)", what, h);
+        return EG_ERR_TIMEOUT;
+    }
+    return EG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// scan of u32 counts into inclusive u64 offsets: out[i] = sum(in[0..i]), out[n] = total
+struct LoadU32 {
+    const uint32_t* p;
+    __device__ uint32_t operator()(uint64_t i) const { return p[i]; }
+};
+struct EpiInclusive {
+    uint64_t* out;
+    __device__ void operator()(uint64_t i, uint64_t excl, uint32_t v) const { out[i] = excl + v; }
+};
+
+int scan_u32_to_u64(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out_incl, uint64_t* total_dev) {
+    return launch_scan(g, LoadU32{in}, EpiInclusive{out_incl}, n, total_dev, "scan_offsets");
+}
+
+// ---------------------------------------------------------------------------------------------
+// compressed incoming index (core/graph.hpp:1144-1188): one (vertex, start) per non-empty list
+// (p, v) plus a sentinel (V, partition end) per partition; cnt holds P*(V+1) counts with the
+// (V+1)-th slot of each partition as the sentinel slot.
+struct LoadFlag {
+    const uint32_t* cnt;
+    uint32_t V;
+    int single;  // P == 1: cnt has V entries, slot V is the sentinel
+    __device__ uint32_t operator()(uint64_t i) const {
+        uint64_t r = single ? i : i % ((uint64_t)V + 1);
+        if (r == V) return 1u;
+        return cnt[i] > 0 ? 1u : 0u;
+    }
+};
+struct EpiCompress {
+    const uint64_t* off;
+    uint32_t* cvert;
+    uint64_t* cidx;
+    uint64_t* cstart;
+    uint32_t V;
+    int single;
+    const uint32_t* cnt;
+    __device__ void operator()(uint64_t i, uint64_t excl, uint32_t flag) const {
+        if (!flag) return;
+        uint64_t r = single ? i : i % ((uint64_t)V + 1);
+        cvert[excl] = r == V ? V : (uint32_t)r;
+        cidx[excl] = off[i];
+        if (r == V) cstart[single ? 1 : i / ((uint64_t)V + 1) + 1] = excl + 1;
+    }
+};
+
+int compress_index(eg_graph* g, const uint32_t* cnt, uint64_t n, uint32_t V, const uint64_t* off, uint32_t* cvert,
+                   uint64_t* cidx, uint64_t* cstart_dev) {
+    int single = n == (uint64_t)V + 1;
+    return launch_scan(g, LoadFlag{cnt, V, single}, EpiCompress{off, cvert, cidx, cstart_dev, V, single, cnt}, n,
+                       nullptr, "compress_index");
+}
+
+// ---------------------------------------------------------------------------------------------
+// R-MAT generator
+__global__ void k_rmat(eg_rmat_params p, uint8_t* out, int rec, uint64_t E) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < E; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t s, d;
+        float w = 0.f;
+        eg_rmat_edge(&p, i, &s, &d, rec == 12 ? &w : nullptr);
+        uint32_t* r = reinterpret_cast<uint32_t*>(out + i * (uint64_t)rec);
+        r[0] = s;
+        r[1] = d;
+        if (rec == 12) r[2] = __float_as_uint(w);
+    }
+}
+
+}  // namespace eg
+
+extern "C" int eg_generate_rmat(void* d_edges, int edge_bytes, uint64_t E, uint32_t V, double a, double b, double c,
+                                uint64_t seed, int permute, float w_lo, float w_hi, void* stream) {
+    if (!d_edges && E) { eg::set_error("eg_generate_rmat: null output"); return EG_ERR_INVALID; }
+    if (edge_bytes != 8 && edge_bytes != 12) { eg::set_error("eg_generate_rmat: edge_bytes must be 8 or 12"); return EG_ERR_INVALID; }
+    if (V == 0) { eg::set_error("eg_generate_rmat: V must be positive"); return EG_ERR_INVALID; }
+    if (!(a >= 0 && b >= 0 && c >= 0 && a + b + c < 1.0)) { eg::set_error("eg_generate_rmat: need a,b,c >= 0, a+b+c < 1"); return EG_ERR_INVALID; }
+    if (E == 0) return EG_OK;
+    eg_rmat_params p;
+    eg_rmat_init(&p, V, E, a, b, c, seed, (uint32_t)(permute != 0), w_lo, w_hi);
+    eg::k_rmat<<<eg::grid_for(E, 256, 152u * 32u), 256, 0, (cudaStream_t)stream>>>(p, (uint8_t*)d_edges, edge_bytes, E);
+    EG_CHECK_LAUNCH("k_rmat");
+    return EG_OK;
+}

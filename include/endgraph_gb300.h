@@ -1,0 +1,167 @@
+/*
+ * endgraph_gb300.h — C ABI of libendgraph_gb300.so: EndGraph preprocessing (CPBT partitioning,
+ * two-level CSR/CSC construction) and the Gemini process_edges toolkits on one GB300 GPU.
+ *
+ * The reference exposes these as the C++ template class Graph<EdgeData> (core/graph.hpp:100) and
+ * the toolkits' compute() functions; it has no C ABI.  Each entry point below names the reference
+ * interface it replaces.  include/core/graph.hpp re-creates the Graph<EdgeData> surface on top of
+ * this ABI.
+ *
+ * Conventions
+ *  - Every function returns an eg_status; eg_last_error() gives the message of the calling
+ *    thread's last failure.  Invalid sizes / pointers are rejected before any GPU work.
+ *  - A handle owns one graph resident in device memory and one CUDA stream; calls on a handle
+ *    are stream-ordered and must be serialised by the caller (handles are not thread-safe).
+ *  - `where` arguments say where a caller buffer lives: EG_HOST (pageable or pinned host memory,
+ *    copies happen inside the call) or EG_DEVICE (device memory of the handle's GPU).
+ *  - Vertex ids are uint32 (UINT, core/type.hpp:26); edge counts and offsets are uint64.
+ *  - Edge records are the reference's binary format (core/type.hpp:29-43): packed
+ *    {uint32 src, uint32 dst} (8 bytes) or {uint32 src, uint32 dst, float w} (12 bytes).
+ */
+#ifndef ENDGRAPH_GB300_H
+#define ENDGRAPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum eg_status {
+    EG_OK = 0,
+    EG_ERR_INVALID = 1,       /* bad argument (size, pointer, id out of range) */
+    EG_ERR_CUDA = 2,          /* CUDA runtime error */
+    EG_ERR_NOMEM = 3,         /* device or pinned allocation failed */
+    EG_ERR_STATE = 4,         /* call out of order (e.g. analytics before eg_build) */
+    EG_ERR_TIMEOUT = 5,       /* a bounded device wait gave up; context stays usable */
+    EG_ERR_HOST_CALLBACK = 6, /* host std::function callbacks cannot run on the device engine */
+    EG_ERR_UNSUPPORTED = 7
+} eg_status;
+
+enum { EG_HOST = 0, EG_DEVICE = 1 };
+
+typedef struct eg_graph eg_graph;
+
+typedef struct eg_config {
+    uint64_t eta;          /* CPBT coefficient, Graph(int eta) core/graph.hpp:202-212 */
+    int32_t partitions;    /* virtual partitions k (MPI world size in the reference), >= 1 */
+    int32_t sub_partitions;/* second-level split per partition (sockets_num), >= 1 */
+    int32_t max_iterations;/* T of the CPBT page weight (core/graph.hpp:733-738) */
+    int32_t device;        /* CUDA device ordinal */
+    void* stream;          /* cudaStream_t to run on; NULL: the handle creates its own */
+} eg_config;
+
+typedef struct eg_info {
+    uint32_t V;
+    uint32_t partitions;
+    uint64_t E;            /* edges after symmetrisation */
+    uint64_t ncompressed;  /* compressed CSC entries incl. one sentinel per partition */
+    int32_t weighted;
+    int32_t built_csr;
+    int32_t built_csc;
+    int32_t symmetric;
+} eg_info;
+
+/* Device views of the built structures (pointers into the handle's memory; valid until the next
+ * load/build or eg_destroy).  Partition p of the CSR holds the edges whose dst it owns, keyed by
+ * src (prepare_push_mode core/graph.hpp:1248-1355); partition p of the CSC holds the edges whose
+ * src it owns, keyed by dst (prepare_pull_mode :1098-1242). */
+typedef struct eg_csr_view {
+    const uint64_t* off;     /* [P*(V+1)] absolute edge positions; list (p,v) = [off[p*(V+1)+v], off[p*(V+1)+v+1]) */
+    const uint32_t* adj;     /* [E] neighbour (dst) */
+    const float* w;          /* [E] or NULL */
+    const uint64_t* bitmap;  /* [P*(V/64+1)] outgoing_adj_bitmap: bit u set iff list (p,u) is non-empty */
+} eg_csr_view;
+
+typedef struct eg_csc_view {
+    const uint64_t* off;     /* [P*(V+1)] dense offsets */
+    const uint32_t* adj;     /* [E] neighbour (src) */
+    const float* w;          /* [E] or NULL */
+    const uint32_t* cvert;   /* [ncompressed] compressed_incoming_adj_index .vertex (sentinel: V) */
+    const uint64_t* cidx;    /* [ncompressed] .index (absolute edge position; sentinel: partition end) */
+} eg_csc_view;
+
+typedef struct eg_kernel_stat {
+    char name[48];
+    uint64_t launches;
+    double ms;
+} eg_kernel_stat;
+
+/* ---- lifetime: Graph(int eta) + init(), core/graph.hpp:202-285 ------------------------------ */
+int eg_create(eg_graph** out, const eg_config* cfg);
+int eg_destroy(eg_graph* g);
+const char* eg_last_error(void);
+int eg_version(void);
+void* eg_stream(eg_graph* g); /* the cudaStream_t all work of g is ordered on */
+int eg_sync(eg_graph* g);
+
+/* ---- loading: preload_graph_file core/graph.hpp:1011-1084 --------------------------------- */
+/* Copies E records (edge_bytes 8 or 12) into device memory; symmetric appends reversed copies
+ * (load_undirected_from_directed, :629-646, :1057-1078).  Ids >= V are rejected (EG_ERR_INVALID). */
+int eg_load_edges(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int symmetric,
+                  int where);
+
+/* ---- preprocessing: split_graph core/graph.hpp:981-1009 ---------------------------------- */
+/* Degree histogram, CPBT partition (assign_vertices :662-792, dense out-degree weights with
+ * T = max_iterations), then the CSR (:1248-1355) and/or CSC (:1098-1242). */
+int eg_build(eg_graph* g, int want_csr, int want_csc);
+/* load_directed core/graph.hpp:1358-1373 = eg_load_edges + eg_build(1, 1) */
+int eg_load_directed(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int where);
+/* load_undirected_from_directed core/graph.hpp:629-646 */
+int eg_load_undirected_from_directed(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes,
+                                     int where);
+
+int eg_get_info(eg_graph* g, eg_info* out);
+/* partition_offset [P+1] (core/graph.hpp:743-749) and local_partition_offset [P*(S+1)] (:774-780,
+ * evaluated for every partition).  Host buffers; either may be NULL. */
+int eg_get_partition(eg_graph* g, uint32_t* partition_offset, uint32_t* local_offset);
+/* out-degree / in-degree arrays [V] (degree[], core/graph.hpp:689-707); either may be NULL. */
+int eg_get_degrees(eg_graph* g, uint32_t* outdeg, uint32_t* indeg, int where);
+int eg_get_csr(eg_graph* g, eg_csr_view* out);
+int eg_get_csc(eg_graph* g, eg_csc_view* out);
+/* Copies of the structures into caller buffers (sizes as in the views; NULL skips an array).
+ * The reference hands these out as per-socket arrays: outgoing_adj_index / _list / _bitmap
+ * (core/graph.hpp:160-163) and incoming_adj_list + compressed_incoming_adj_index (:158-168). */
+int eg_copy_csr(eg_graph* g, uint64_t* off, uint32_t* adj, float* w, uint64_t* bitmap, int where);
+int eg_copy_csc(eg_graph* g, uint64_t* off, uint32_t* adj, float* w, uint32_t* cvert, uint64_t* cidx, int where);
+
+/* ---- CPBT on its own: assign_vertices / optimal_offset core/graph.hpp:586-792 ------------- */
+/* deg: [V] degrees (where says host or device).  dense selects T = max_iterations. */
+int eg_cpbt_partition(const uint32_t* deg, uint32_t V, int P, int S, uint64_t eta, int max_iterations, int dense,
+                      int where, uint32_t* partition_offset, uint32_t* local_offset);
+/* optimal_offset(a, n, k) core/graph.hpp:597-626 on the GPU; a on the host, offset[k+1] on host. */
+int eg_optimal_offset(const uint64_t* a, uint32_t n, uint32_t k, uint32_t* offset);
+
+/* ---- toolkits: process_edges / process_vertices core/graph.hpp:1376-1817 ------------------ */
+/* Gemini PageRank (toolkits/pagerank.cpp:26-98): dense pull every iteration, FP32 ranks.
+ * out[V] receives the final curr array. */
+int eg_pagerank(eg_graph* g, int iterations, float damping, float* out, int where);
+/* BFS (toolkits/bfs.cpp:22-84), push.  level[V] (0xFFFFFFFF unreached) and parent[V] (V when
+ * unreached; parent[root] = root); either may be NULL.  *reached (may be NULL) = reached count. */
+int eg_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int where, uint64_t* reached);
+/* CC (toolkits/cc.cpp:22-84) on a graph loaded with eg_load_undirected_from_directed: min-label
+ * propagation, push/pull switched per iteration on active_edges < E/20 (core/graph.hpp:1484-1491). */
+int eg_cc(eg_graph* g, uint32_t* label, int where);
+/* SSSP (toolkits/sssp.cpp:24-84), push Bellman-Ford on float weights; unreached = 1e9. */
+int eg_sssp(eg_graph* g, uint32_t root, float* dist, int where);
+
+/* statistics of the last toolkit call: edges traversed, iterations, push / pull iterations */
+int eg_last_run(eg_graph* g, uint64_t* edges_processed, int* iterations, int* push_iters, int* pull_iters);
+
+/* ---- synthetic input (no reference counterpart; include/endgraph_rmat.h) ------------------ */
+/* Writes E records of the seeded R-MAT stream into device memory (edge_bytes 8 or 12). */
+int eg_generate_rmat(void* d_edges, int edge_bytes, uint64_t E, uint32_t V, double a, double b, double c,
+                     uint64_t seed, int permute, float w_lo, float w_hi, void* stream);
+
+/* ---- profiling: per-kernel CUDA-event timing on the handle's stream ----------------------- */
+int eg_profile_enable(eg_graph* g, int enable);
+int eg_profile_reset(eg_graph* g);
+/* fills up to cap entries, returns the number of kernels via *count */
+int eg_profile_read(eg_graph* g, eg_kernel_stat* out, int cap, int* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ENDGRAPH_GB300_H */

@@ -1,0 +1,148 @@
+"""GPU parity: libendgraph_gb300 (through its C ABI) against the CPU oracle on seeded R-MAT graphs."""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import lists_equal, rel_l1, rmat_graph
+
+pytestmark = pytest.mark.gpu
+
+CASES = [  # (V, E, seed)
+    (1 << 12, 1 << 16, 1),
+    (1 << 16, 1 << 20, 2),
+    (100_000, 300_000, 3),   # V not a page multiple
+    (5000, 30_000, 4),
+]
+
+
+def _graph(eg_lib, P=1, S=1, eta=1, T=20):
+    import endgraph_gb300 as eg
+    return eg.Graph(eta=eta, partitions=P, sub_partitions=S, max_iterations=T)
+
+
+@pytest.mark.parametrize("V,E,seed", CASES)
+def test_structure_single_partition(eg_lib, V, E, seed):
+    import endgraph_gb300 as eg
+    src, dst, _ = rmat_graph(V, E, seed)
+    with _graph(eg_lib) as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        outd, ind = g.degrees()
+        o_out, o_in = oracle.degrees(src, dst, V)
+        assert np.array_equal(outd, o_out) and np.array_equal(ind, o_in)
+        po, lo = g.partition()
+        opo, olo = oracle.cpbt(o_out, V, 1, 1, 1, 20, True)
+        assert np.array_equal(po, opo) and np.array_equal(lo, olo)
+        ref_csr = oracle.build_csr(src, dst, None, V, opo)
+        ref_csc = oracle.build_csc(src, dst, None, V, opo)
+        csr = g.csr()
+        csc = g.csc()
+        assert lists_equal(csr["off"][0], csr["adj"], ref_csr["off"][0], ref_csr["adj"])
+        assert np.array_equal(csr["bitmap"], ref_csr["bitmap"])
+        assert lists_equal(csc["off"][0], csc["adj"], ref_csc["off"][0], ref_csc["adj"])
+        assert np.array_equal(csc["cvert"], ref_csc["cvert"])
+        assert np.array_equal(csc["cidx"], ref_csc["cidx"])
+
+
+@pytest.mark.parametrize("P,S", [(2, 1), (3, 2), (8, 3), (16, 1)])
+def test_structure_partitions(eg_lib, P, S):
+    import endgraph_gb300 as eg
+    V, E = 1 << 16, 1 << 19
+    src, dst, w = rmat_graph(V, E, 11 + P, weights=(0.0, 1.0))
+    with _graph(eg_lib, P=P, S=S, eta=3) as g:
+        g.load_directed(eg.pack_edges(src, dst, w), V)
+        o_out, _ = oracle.degrees(src, dst, V)
+        opo, olo = oracle.cpbt(o_out, V, P, S, 3, 20, True)
+        po, lo = g.partition()
+        assert np.array_equal(po, opo) and np.array_equal(lo, olo)
+        ref_csr = oracle.build_csr(src, dst, w, V, opo)
+        ref_csc = oracle.build_csc(src, dst, w, V, opo)
+        csr, csc = g.csr(), g.csc()
+        for p in range(P):
+            assert lists_equal(csr["off"][p], csr["adj"], ref_csr["off"][p], ref_csr["adj"], csr["w"], ref_csr["w"])
+            assert lists_equal(csc["off"][p], csc["adj"], ref_csc["off"][p], ref_csc["adj"], csc["w"], ref_csc["w"])
+        assert np.array_equal(csr["bitmap"], ref_csr["bitmap"])
+        assert np.array_equal(csc["cvert"], ref_csc["cvert"])
+        assert np.array_equal(csc["cidx"], ref_csc["cidx"])
+
+
+@pytest.mark.parametrize("V,E,seed", CASES)
+@pytest.mark.parametrize("P", [1, 3])
+def test_pagerank(eg_lib, V, E, seed, P):
+    import endgraph_gb300 as eg
+    src, dst, _ = rmat_graph(V, E, seed)
+    o_out, _ = oracle.degrees(src, dst, V)
+    csc = oracle.build_csc(src, dst, None, V, np.array([0, V], np.uint32))
+    ref = oracle.pagerank(csc["off"][0], csc["adj"], o_out, V, 20, 0.85)
+    with _graph(eg_lib, P=P) as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        pr = g.pagerank(20, 0.85)
+    err = rel_l1(pr, ref)
+    assert err <= 1e-6, err
+
+
+@pytest.mark.parametrize("V,E,seed", CASES)
+@pytest.mark.parametrize("P", [1, 2])
+def test_bfs(eg_lib, V, E, seed, P):
+    import endgraph_gb300 as eg
+    src, dst, _ = rmat_graph(V, E, seed)
+    csr = oracle.build_csr(src, dst, None, V, np.array([0, V], np.uint32))
+    with _graph(eg_lib, P=P) as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        for root in [int(src[0]), int(src[len(src) // 2]), 0]:
+            lv_ref = oracle.bfs_levels(csr["off"][0], csr["adj"], V, root)
+            lv, par = g.bfs(root)
+            assert np.array_equal(lv, lv_ref)
+            assert oracle.bfs_check_parents(csr["off"][0], csr["adj"], V, root, lv, par) == 0
+
+
+@pytest.mark.parametrize("V,E,seed", CASES)
+def test_cc(eg_lib, V, E, seed):
+    import endgraph_gb300 as eg
+    src, dst, _ = rmat_graph(V, E, seed)
+    ref = oracle.cc_labels(src, dst, V)
+    with _graph(eg_lib) as g:
+        g.load_undirected_from_directed(eg.pack_edges(src, dst), V)
+        lab = g.cc()
+        assert np.array_equal(lab, ref)
+
+
+@pytest.mark.parametrize("V,E,seed", CASES)
+def test_sssp(eg_lib, V, E, seed):
+    import endgraph_gb300 as eg
+    src, dst, w = rmat_graph(V, E, seed, weights=(0.0, 1.0))
+    csr = oracle.build_csr(src, dst, w, V, np.array([0, V], np.uint32))
+    with _graph(eg_lib) as g:
+        g.load_directed(eg.pack_edges(src, dst, w), V)
+        for root in [int(src[0]), int(src[7])]:
+            ref = oracle.sssp(csr["off"][0], csr["adj"], csr["w"], V, root)
+            d = g.sssp(root)
+            assert np.array_equal(d.view(np.uint32), ref.view(np.uint32))
+
+
+def test_generator_matches_host(eg_lib):
+    import torch
+    import endgraph_gb300 as eg
+    V, E = 100_003, 1 << 16
+    for weights in [None, (0.5, 1.5)]:
+        out = torch.empty((E, 3 if weights else 2), dtype=torch.int32, device="cuda")
+        eg.generate_rmat(out, V, E, 99, weights=weights)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().view(np.uint32)
+        src, dst, w = oracle.rmat(V, E, 99, weights=weights)
+        assert np.array_equal(got[:, 0], src) and np.array_equal(got[:, 1], dst)
+        if weights:
+            assert np.array_equal(got[:, 2], w.view(np.uint32))
+
+
+def test_cpbt_kats(eg_lib):
+    import endgraph_gb300 as eg
+    a = [5, 0, 0, 7, 1, 0, 9, 3, 0, 2]
+    assert list(eg.optimal_offset(a, 2)) == [0, 6, 10]
+    assert list(eg.optimal_offset(a, 4)) == [0, 3, 6, 7, 10]
+    assert list(eg.optimal_offset(a, 5)) == [0, 3, 6, 7, 10, 10]
+    assert list(eg.optimal_offset([0, 0, 0, 0], 3)) == [0, 4, 4, 4]
+    rng = np.random.default_rng(5)
+    for n in [1, 2, 17, 1000, 30000]:
+        for k in [1, 2, 3, 7, 64]:
+            w = rng.integers(0, 1 << 40, n, dtype=np.uint64) * (rng.random(n) < 0.8)
+            assert np.array_equal(eg.optimal_offset(w, k), oracle.optimal_offset(w, k)), (n, k)
