@@ -1,0 +1,381 @@
+"""Benchmark: EndGraph preprocessing (CPBT + CSR + CSC) and the Gemini toolkits on one GB300.
+
+Workload (the reference's preprocessing-at-scale configuration): R-MAT with V = 2^25 vertices and
+E = 2^29 edges (a=0.57, b=0.19, c=0.19, d=0.05, seeded, vertex ids permuted), uint32 ids.
+One step = load_directed's preprocessing (CPBT partition + CSR + CSC from the edge list resident in
+HBM; file/ingest excluded like the reference's prep_time) + PageRank 20 iterations (FP32) + BFS from
+16 random non-isolated roots.  value = E / t_prep in Medges/s; PageRank and BFS GTEPS ride along.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's own engine (oracle/_ref, built from the reference sources at
+one rank with all host threads) on the same metric.  With N > 1 (torchrun) every rank runs an
+independent replica (the path is single-GPU; "replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+A, B, C = 0.57, 0.19, 0.19
+SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--scale", type=int, default=25)
+    p.add_argument("--edge-factor", type=int, default=16)
+    p.add_argument("--pr-iters", type=int, default=20)
+    p.add_argument("--roots", type=int, default=16)
+    p.add_argument("--seed", type=int, default=20240601)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 100 ms) while the timed region runs."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={SMI_FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, power, reasons = [], None, [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        loaded = [s for s, p in zip(sm, power) if p >= 0.5 * max(power)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": max(power)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------------------------
+def reference_prep(V, E, seed, threads_note=True, steps=1, warmup=0):
+    """Time the reference's own preprocessing (oracle/_ref) on host cores; returns seconds list."""
+    import oracle
+    if not oracle.Reference.available():
+        if oracle.build_ref() is None:
+            return None, "reference engine not built (reference sources absent on this machine)"
+    src, dst, _ = oracle.rmat(V, E, seed, a=A, b=B, c=C, permute=True)
+    times = []
+    for i in range(warmup + steps):
+        R = oracle.Reference(src, dst, None, V, eta=1, max_iterations=20)
+        t = R.build()
+        R.close()
+        if i >= warmup:
+            times.append(t)
+    return times, int(oracle.Reference.lib().ref_threads())
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    V = 1 << args.scale
+    E = V * args.edge_factor
+    # bounded sample: the same generator at 1/8 of the edges and vertices (edge factor kept)
+    sv, se = V >> 3, E >> 3
+    times, threads = reference_prep(sv, se, args.seed, steps=args.steps, warmup=args.warmup)
+    if times is None:
+        print(json.dumps({"impl": "reference", "unavailable": threads}))
+        return
+    t = sum(times) / len(times)
+    value = se / t / 1e6
+    line = {
+        "impl": "reference", "metric": "preproc Medges/s", "value": round(value, 3), "unit": "Medges/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"rmat-s{args.scale}-ef{args.edge_factor} CPBT+CSR+CSC (load_directed)",
+                   "V": V, "E": E, "seed": args.seed},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Medges/s", "cores": threads, "kind": "reference",
+                         "sample": f"R-MAT V=2^{args.scale - 3}, E=2^{(E >> 3).bit_length() - 1} (same generator "
+                                   f"and edge factor, 1/8 of the workload), prep_time of split_graph per step"},
+        "e2e": {"value": round(value, 3), "unit": "Medges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------------------------
+ALG_BYTES = {  # algorithmic bytes per launch (E edges, V vertices, nc compressed entries)
+    "degrees": lambda E, V, nc: 8 * E + 8 * V,
+    "scatter": lambda E, V, nc: 16 * E + 32 * V,
+    "scan_offsets": lambda E, V, nc: 12 * V,
+    "compress_index": lambda E, V, nc: 12 * V + 12 * nc,
+    "bitmap": lambda E, V, nc: 4 * V + V // 8,
+    "cpbt_page_weights": lambda E, V, nc: 4 * V,
+    "pr_pull": lambda E, V, nc: 8 * E + 16 * nc,
+}
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    import endgraph_gb300 as eg
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    V = 1 << args.scale
+    E = V * args.edge_factor
+    seed = args.seed + rank
+    peak, peak_kind = measured_peaks()
+
+    edges = torch.empty((E, 2), dtype=torch.int32, device=dev)
+    eg.generate_rmat(edges, V, E, seed, A, B, C, permute=True)
+    torch.cuda.synchronize()
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    ridx = torch.randint(0, E, (args.roots,), generator=gen)
+    roots = [int(x) for x in edges[ridx.to(dev), 0].cpu().numpy().view(np.uint32)]
+
+    g = eg.Graph(eta=1, partitions=1, max_iterations=args.pr_iters, device=local)
+    g.load_edges(edges, V)
+    stream = torch.cuda.ExternalStream(g.stream, device=dev)
+    pr_out = torch.empty(V, dtype=torch.float32, device=dev)
+    level = torch.empty(V, dtype=torch.int32, device=dev)
+
+    def step(evs=None):
+        with torch.cuda.stream(stream):
+            if evs:
+                evs[0].record(stream)
+            g.build()
+            if evs:
+                evs[1].record(stream)
+            g.pagerank(args.pr_iters, 0.85, out=pr_out)
+            if evs:
+                evs[2].record(stream)
+            reach = 0
+            for r in roots:
+                g.bfs(r, level=level, want_parent=False)
+                reach += g.last_run()["edges"]
+            if evs:
+                evs[3].record(stream)
+        return reach
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    nc = g.info().ncompressed
+
+    g.profile(True)
+    g.profile_reset()
+    per = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reach_total = 0
+        for k in range(args.steps):
+            reach_total += step(per[k])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        barrier(world)
+    g.profile(False)
+    prof = g.profile_read()
+    prep_ms = [per[k][0].elapsed_time(per[k][1]) for k in range(args.steps)]
+    pr_ms = [per[k][1].elapsed_time(per[k][2]) for k in range(args.steps)]
+    bfs_ms = [per[k][2].elapsed_time(per[k][3]) for k in range(args.steps)]
+    step_ms = [per[k][0].elapsed_time(per[k][3]) for k in range(args.steps)]
+    t_prep = max_over_ranks(sum(prep_ms) / args.steps, world, dev)
+    t_step = max_over_ranks(sum(step_ms) / args.steps, world, dev)
+    value = world * E / (t_prep / 1e3) / 1e6
+
+    # roofline of the dominant kernel (largest device time in the timed region)
+    kern = {k: (n, ms) for k, (n, ms) in prof.items()}
+    dom = max(kern, key=lambda k: kern[k][1])
+    n_dom, ms_dom = kern[dom]
+    alg = ALG_BYTES.get(dom)
+    achieved = None
+    if alg:
+        achieved = alg(E, V, nc) / (ms_dom / n_dom / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tr = json.load(f)
+        if dom in tr:
+            traffic = tr[dom].get("bytes_per_launch_at_bench")
+    prep_bytes = 24 * E + 32 * V
+    pr_bytes = args.pr_iters * (8 * E + 20 * V)
+    kernels = {k: {"launches": n, "ms_total": round(ms, 3), "ms_per_launch": round(ms / n, 4),
+                   "share": round(ms / sum(x[1] for x in kern.values()), 4)} for k, (n, ms) in
+               sorted(kern.items(), key=lambda kv: -kv[1][1])}
+    for k in kernels:
+        if k in ALG_BYTES:
+            gbs = ALG_BYTES[k](E, V, nc) / (kern[k][1] / kern[k][0] / 1e3) / 1e9
+            kernels[k]["alg_GBps"] = round(gbs, 1)
+            kernels[k]["frac_of_peak"] = round(gbs / peak, 4)
+
+    # end to end through the C ABI from pinned host memory: H2D + validation + build + D2H result
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((E, 2), dtype=torch.int32, pin_memory=True)
+        host.copy_(edges)
+        h_np = host.numpy()
+        g2 = eg.Graph(eta=1, partitions=1, max_iterations=args.pr_iters, device=local)
+        g2.load_directed(h_np, V)
+        g2.sync()
+        n_e2e = max(2, min(args.steps, 5))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            g2.load_directed(h_np, V)
+            po, _ = g2.partition()
+        g2.sync()
+        e2e_s = (time.perf_counter() - t0) / n_e2e
+        e2e_s = max_over_ranks(e2e_s, world, dev)
+        e2e = {"value": round(world * E / e2e_s / 1e6, 3), "unit": "Medges/s", "h2d_bytes_per_step": 8 * E,
+               "d2h_bytes_per_step": 4 * len(po) + 64, "ms_per_step": round(e2e_s * 1e3, 3),
+               "path": "eg_load_directed(host pinned records) + eg_get_partition"}
+        g2.close()
+        del host
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sv, se = V >> 3, E >> 3
+        times, threads = reference_prep(sv, se, args.seed, steps=1, warmup=0)
+        if times is not None:
+            cpu = {"value": round(se / times[0] / 1e6, 3), "unit": "Medges/s", "cores": threads,
+                   "kind": "reference",
+                   "sample": f"reference split_graph (CPBT+CSR+CSC) on R-MAT V=2^{args.scale - 3}, "
+                             f"E=2^{(se).bit_length() - 1} (same generator, edge factor {args.edge_factor})"}
+        else:
+            cpu = {"value": None, "unit": "Medges/s", "cores": 0, "kind": "reference", "sample": threads}
+
+    bfs_gteps = reach_total / (sum(bfs_ms) / 1e3) / 1e9
+    pr_gteps = args.pr_iters * E / (sum(pr_ms) / args.steps / 1e3) / 1e9
+    launches = sum(n for n, _ in kern.values())
+    if rank == 0:
+        line = {
+            "metric": "preproc Medges/s", "value": round(value, 3), "unit": "Medges/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": f"rmat-s{args.scale}-ef{args.edge_factor} CPBT+CSR+CSC, PageRank x{args.pr_iters}, "
+                                   f"BFS x{args.roots} roots", "V": V, "E": E, "seed": args.seed,
+                       "partitions": 1, "eta": 1, "l2": "inputs larger than L2 (4 GiB edge list, 2 GiB per structure)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "phases": {"prep_ms": round(t_prep, 3), "prep_medges_s": round(value / world, 1),
+                       "prep_alg_GBps": round(prep_bytes / (t_prep / 1e3) / 1e9, 1),
+                       "prep_frac_of_peak": round(prep_bytes / (t_prep / 1e3) / 1e9 / peak, 4),
+                       "pagerank_ms": round(sum(pr_ms) / args.steps, 3), "pagerank_gteps": round(pr_gteps, 2),
+                       "pagerank_alg_frac_of_peak": round(pr_bytes / (sum(pr_ms) / args.steps / 1e3) / 1e9 / peak, 4),
+                       "bfs_ms_per_root": round(sum(bfs_ms) / args.steps / args.roots, 3),
+                       "bfs_gteps": round(bfs_gteps, 2)},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": None if achieved is None else round(achieved, 1),
+                         "peak": peak, "unit": "GB/s",
+                         "frac": None if achieved is None else round(achieved / peak, 4),
+                         "traffic": traffic, "peak_kind": peak_kind},
+            "kernels": kernels,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "wall_s_timed": round(wall, 3),
+        }
+        print(json.dumps(line))
+    g.close()
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

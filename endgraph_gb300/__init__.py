@@ -21,6 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = _build.LIB
 
 EG_HOST, EG_DEVICE = 0, 1
+EG_OPT_BFS_DIRECTION, EG_OPT_DENSE_DIVISOR = 1, 2
 STATUS = {0: "EG_OK", 1: "EG_ERR_INVALID", 2: "EG_ERR_CUDA", 3: "EG_ERR_NOMEM", 4: "EG_ERR_STATE",
           5: "EG_ERR_TIMEOUT", 6: "EG_ERR_HOST_CALLBACK", 7: "EG_ERR_UNSUPPORTED"}
 
@@ -74,6 +75,7 @@ SIGNATURES = {
     "eg_cc": ([_vp, _vp, _i32], _i32),
     "eg_sssp": ([_vp, _u32, _vp, _i32], _i32),
     "eg_last_run": ([_vp, _vp, _vp, _vp, _vp], _i32),
+    "eg_set_option": ([_vp, _i32, ctypes.c_int64], _i32),
     "eg_generate_rmat": ([_vp, _i32, _u64, _u32, _f64, _f64, _f64, _u64, _i32, _f32, _f32, _vp], _i32),
     "eg_profile_enable": ([_vp, _i32], _i32),
     "eg_profile_reset": ([_vp], _i32),
@@ -281,6 +283,9 @@ class Graph:
         p, where = _buf(dist)
         _check(self._L.eg_sssp(self.h, root, p, where))
         return dist
+
+    def set_option(self, option, value):
+        _check(self._L.eg_set_option(self.h, option, value))
 
     def last_run(self):
         e = ctypes.c_uint64()

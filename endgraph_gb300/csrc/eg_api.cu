@@ -39,6 +39,7 @@ int init_handle(eg_graph* g, const eg_config* cfg) {
     }
     g->device = c.device;
     EG_CUDA(cudaSetDevice(g->device));
+    EG_CUDA(cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->device));
     g->eta = c.eta;
     g->partitions = c.partitions;
     g->sub_partitions = c.sub_partitions;
@@ -327,6 +328,25 @@ int eg_cc(eg_graph* g, uint32_t* label, int where) {
 int eg_sssp(eg_graph* g, uint32_t root, float* dist, int where) {
     EG_TRY(check_graph(g, "eg_sssp"));
     return run_sssp(g, root, dist, where);
+}
+
+int eg_set_option(eg_graph* g, int option, int64_t value) {
+    EG_TRY(check_graph(g, "eg_set_option"));
+    switch (option) {
+        case EG_OPT_BFS_DIRECTION:
+            if (value < 0 || value > 2) break;
+            g->bfs_direction = (int)value;
+            return EG_OK;
+        case EG_OPT_DENSE_DIVISOR:
+            if (value < 1 || value > (1 << 30)) break;
+            g->dense_div = (int)value;
+            return EG_OK;
+        default:
+            set_error("eg_set_option: unknown option %d", option);
+            return EG_ERR_INVALID;
+    }
+    set_error("eg_set_option: value %lld out of range for option %d", (long long)value, option);
+    return EG_ERR_INVALID;
 }
 
 int eg_last_run(eg_graph* g, uint64_t* edges_processed, int* iterations, int* push_iters, int* pull_iters) {

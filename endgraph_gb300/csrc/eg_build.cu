@@ -283,6 +283,336 @@ __global__ void k_part_edges(const uint64_t* off, uint32_t V, int P, uint64_t E,
     if (p == P) out[P] = E;
 }
 
+// =============================================================================================
+// One-partition build without per-edge global atomics: a counting sort in three passes.
+//   A  per-block shared-memory histograms of the bucket (vertex >> shift) of src and of dst
+//   B  each block re-reads its edges and writes them bucket by bucket to offsets given by an
+//      exclusive scan of A's (bucket, block) counts; the 2 x nb x nblk write frontiers advance
+//      sequentially, so L2 merges the scattered record stores into full sectors
+//   C  one CTA per bucket: shared-memory degree histogram of the bucket's vertex range, block scan
+//      (degrees and offsets written coalesced), then the scatter into the bucket's contiguous
+//      output range through shared-memory cursors
+// =============================================================================================
+constexpr int kBucketThreads = 512;
+constexpr int kBuildThreads = 1024;
+constexpr uint32_t kMaxBucketVerts = 16384;
+
+template <int REC>
+__global__ void __launch_bounds__(kBucketThreads) k_bucket_hist(const uint8_t* __restrict__ edges, uint64_t E,
+                                                                 uint64_t chunk, int shift, uint32_t nb, uint32_t nblk,
+                                                                 uint32_t* __restrict__ cnt) {
+    extern __shared__ uint32_t s_h[];  // [2][nb]
+    for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_h[i] = 0;
+    __syncthreads();
+    const uint64_t e0 = blockIdx.x * chunk;
+    const uint64_t e1 = e0 + chunk < E ? e0 + chunk : E;
+    if (REC == 8) {
+        // two records per 16-byte load (chunk is even, the buffer is 16-byte aligned)
+        const uint4* p = reinterpret_cast<const uint4*>(edges);
+        for (uint64_t e = e0 + 2 * threadIdx.x; e < e1; e += 2 * blockDim.x) {
+            if (e + 1 < e1) {
+                uint4 x = __ldcs(p + e / 2);
+                atomicAdd(&s_h[x.x >> shift], 1u);
+                atomicAdd(&s_h[nb + (x.y >> shift)], 1u);
+                atomicAdd(&s_h[x.z >> shift], 1u);
+                atomicAdd(&s_h[nb + (x.w >> shift)], 1u);
+            } else {
+                uint2 x = reinterpret_cast<const uint2*>(edges)[e];
+                atomicAdd(&s_h[x.x >> shift], 1u);
+                atomicAdd(&s_h[nb + (x.y >> shift)], 1u);
+            }
+        }
+    } else {
+        for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            uint32_t s, d;
+            float w;
+            load_edge<REC>(edges, e, s, d, w);
+            atomicAdd(&s_h[s >> shift], 1u);
+            atomicAdd(&s_h[nb + (d >> shift)], 1u);
+        }
+    }
+    __syncthreads();
+    // bucket-major layout: [half][bucket][block]
+    for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) cnt[(uint64_t)i * nblk + blockIdx.x] = s_h[i];
+}
+
+template <int REC>
+__device__ __forceinline__ void store_rec(uint8_t* out, uint64_t pos, uint32_t s, uint32_t d, float w) {
+    if (REC == 8) {
+        reinterpret_cast<uint2*>(out)[pos] = make_uint2(s, d);
+    } else {
+        uint32_t* r = reinterpret_cast<uint32_t*>(out + pos * 12u);
+        r[0] = s;
+        r[1] = d;
+        r[2] = __float_as_uint(w);
+    }
+}
+
+// in-place exclusive scan of s[0..n) by the whole block; returns the total
+__device__ uint32_t block_exclusive_scan(uint32_t* s, uint32_t n, uint32_t* s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t b0 = threadIdx.x * per;
+    uint32_t tsum = 0;
+    for (uint32_t j = 0; j < per; ++j)
+        if (b0 + j < n) tsum += s[b0 + j];
+    uint32_t inc = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    uint32_t wb = 0, total = 0;
+    for (int w = 0; w < nw; ++w) {
+        uint32_t x = s_warp[w];
+        if (w < warp) wb += x;
+        total += x;
+    }
+    uint32_t run = wb + inc - tsum;
+    for (uint32_t j = 0; j < per; ++j) {
+        if (b0 + j < n) {
+            uint32_t c = s[b0 + j];
+            s[b0 + j] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    return total;
+}
+
+// B: tiles of kScatterPer x 1024 edges are counting-sorted by bucket in shared memory and then
+// stored in that order, so consecutive threads store consecutive addresses of a bucket's run
+// (whole sectors instead of one partial sector per record).  The block's running base per bucket
+// starts at its exclusive (bucket, block) offset from the scan of pass A.
+constexpr int kScatterThreads = 1024;
+constexpr int kScatterPer = 8;
+constexpr int kScatterTile = kScatterThreads * kScatterPer;
+
+template <int REC>
+__global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_t* __restrict__ edges, uint64_t E,
+                                                                    uint64_t chunk, int shift, uint32_t nb, uint32_t nblk,
+                                                                    const uint64_t* __restrict__ excl,
+                                                                    uint8_t* __restrict__ out) {
+    constexpr int W = REC / 4;  // words per record
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    unsigned long long* s_base = reinterpret_cast<unsigned long long*>(s_raw);  // [2][nb]
+    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_base + 2 * nb);            // [nb]
+    uint32_t* s_stage = s_cnt + nb;                                               // [tile][W]
+    __shared__ uint32_t s_warp[32];
+    for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_base[i] = excl[(uint64_t)i * nblk + blockIdx.x];
+    const uint64_t e0 = blockIdx.x * chunk;
+    const uint64_t e1 = e0 + chunk < E ? e0 + chunk : E;
+    for (uint64_t t0 = e0; t0 < e1; t0 += kScatterTile) {
+        uint32_t rec[kScatterPer][W];
+        bool valid[kScatterPer];
+#pragma unroll
+        for (int j = 0; j < kScatterPer; ++j) {
+            const uint64_t e = t0 + (uint64_t)j * blockDim.x + threadIdx.x;
+            valid[j] = e < e1;
+            if (valid[j]) {
+                const uint32_t* r = reinterpret_cast<const uint32_t*>(edges + e * REC);
+#pragma unroll
+                for (int w = 0; w < W; ++w) rec[j][w] = __ldcs(r + w);
+            }
+        }
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) s_cnt[i] = 0;
+            __syncthreads();
+            uint32_t rank[kScatterPer];
+#pragma unroll
+            for (int j = 0; j < kScatterPer; ++j)
+                rank[j] = valid[j] ? atomicAdd(&s_cnt[rec[j][half] >> shift], 1u) : 0u;
+            __syncthreads();
+            // tile-local exclusive starts; s_cnt keeps the counts in a copy inside s_stage's tail
+            const uint32_t n_tile = block_exclusive_scan(s_cnt, nb, s_warp);
+#pragma unroll
+            for (int j = 0; j < kScatterPer; ++j) {
+                if (valid[j]) {
+                    const uint32_t slot = s_cnt[rec[j][half] >> shift] + rank[j];
+#pragma unroll
+                    for (int w = 0; w < W; ++w) s_stage[slot * W + w] = rec[j][w];
+                }
+            }
+            __syncthreads();
+            unsigned long long* base = s_base + (size_t)half * nb;
+            for (uint32_t i = threadIdx.x; i < n_tile; i += blockDim.x) {
+                const uint32_t* r = s_stage + i * W;
+                const uint32_t b = r[half] >> shift;
+                const uint64_t pos = base[b] + (i - s_cnt[b]);
+                uint32_t* o = reinterpret_cast<uint32_t*>(out + pos * REC);
+#pragma unroll
+                for (int w = 0; w < W; ++w) o[w] = r[w];
+            }
+            __syncthreads();
+            // advance the block's running bases by this tile's counts (start[b+1] - start[b])
+            for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
+                const uint32_t next = b + 1 < nb ? s_cnt[b + 1] : n_tile;
+                base[b] += next - s_cnt[b];
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// C: one bucket per CTA iteration (persistent CTAs take buckets from a ticket)
+template <int REC>
+__global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* __restrict__ rec, const uint64_t* __restrict__ excl,
+                                                                 uint64_t half_base, uint64_t E, uint32_t nb, uint32_t nblk,
+                                                                 uint32_t LB, uint32_t V, int key_is_src,
+                                                                 uint32_t* __restrict__ deg, uint64_t* __restrict__ off,
+                                                                 uint32_t* __restrict__ adj, float* __restrict__ wout,
+                                                                 uint32_t* ticket) {
+    extern __shared__ uint32_t s_cnt[];  // LB counters
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_b;
+    while (true) {
+        if (threadIdx.x == 0) s_b = atomicAdd(ticket, 1u);
+        __syncthreads();
+        const uint32_t b = s_b;
+        if (b >= nb) break;
+        const uint32_t v0 = b * LB;
+        const uint32_t nv = V - v0 < LB ? V - v0 : LB;
+        const uint64_t r0 = excl[(uint64_t)b * nblk] - half_base;
+        const uint64_t r1 = b + 1 < nb ? excl[(uint64_t)(b + 1) * nblk] - half_base : E;
+        for (uint32_t i = threadIdx.x; i < nv; i += blockDim.x) s_cnt[i] = 0;
+        __syncthreads();
+        for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+            const uint32_t* p = reinterpret_cast<const uint32_t*>(rec + r * REC);
+            const uint32_t key = (key_is_src ? p[0] : p[1]) - v0;
+            atomicAdd(&s_cnt[key], 1u);
+        }
+        __syncthreads();
+        // degrees out, then offsets from the block scan
+        for (uint32_t i = threadIdx.x; i < nv; i += blockDim.x) deg[v0 + i] = s_cnt[i];
+        __syncthreads();
+        block_exclusive_scan(s_cnt, nv, s_warp);
+        for (uint32_t i = threadIdx.x; i < nv; i += blockDim.x) off[v0 + i] = r0 + s_cnt[i];
+        if (threadIdx.x == 0 && v0 + nv == V) off[V] = r1;
+        __syncthreads();
+        for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+            const uint32_t* p = reinterpret_cast<const uint32_t*>(rec + r * REC);
+            const uint32_t s = p[0], d = p[1];
+            const uint32_t key = (key_is_src ? s : d) - v0;
+            const uint64_t pos = r0 + atomicAdd(&s_cnt[key], 1u);
+            adj[pos] = key_is_src ? d : s;
+            if (REC == 12) wout[pos] = __uint_as_float(p[2]);
+        }
+        __syncthreads();
+    }
+}
+
+struct BucketPlan {
+    int shift;
+    uint32_t LB, nb, nblk;
+    uint64_t chunk;
+};
+
+static BucketPlan plan_buckets(uint32_t V, uint64_t E) {
+    BucketPlan p;
+    uint32_t lb = 256;
+    while (lb < kMaxBucketVerts && (uint64_t)lb * 1024 < V) lb <<= 1;  // aim for >= 1024 buckets
+    p.LB = lb;
+    p.shift = 0;
+    while ((1u << p.shift) < lb) ++p.shift;
+    p.nb = (uint32_t)(((uint64_t)V + lb - 1) / lb);
+    uint64_t want = (E + 65535) / 65536;
+    p.nblk = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, 304));
+    p.chunk = (E + p.nblk - 1) / p.nblk;
+    p.chunk = (p.chunk + 63) & ~63ull;
+    p.nblk = (uint32_t)std::max<uint64_t>(1, (E + p.chunk - 1) / p.chunk);
+    return p;
+}
+
+int scan_exclusive_u32(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out);
+
+static int build_single(eg_graph* g, int want_csr, int want_csc) {
+    const uint32_t V = g->V;
+    const uint64_t E = g->E;
+    const int rec = g->edge_bytes;
+    EG_TRY(g->outdeg.reserve(sizeof(uint32_t) * (size_t)V));
+    EG_TRY(g->indeg.reserve(sizeof(uint32_t) * (size_t)V));
+    EG_TRY(g->csr_off.reserve(sizeof(uint64_t) * ((size_t)V + 1)));
+    EG_TRY(g->csc_off.reserve(sizeof(uint64_t) * ((size_t)V + 1)));
+    EG_TRY(g->csr_adj.reserve(sizeof(uint32_t) * (E + 32)));
+    EG_TRY(g->csc_adj.reserve(sizeof(uint32_t) * (E + 32)));
+    if (g->weighted) {
+        EG_TRY(g->csr_w.reserve(sizeof(float) * (E + 32)));
+        EG_TRY(g->csc_w.reserve(sizeof(float) * (E + 32)));
+    }
+    if (E == 0) {
+        EG_CUDA(cudaMemsetAsync(g->outdeg.ptr, 0, sizeof(uint32_t) * (size_t)V, g->stream));
+        EG_CUDA(cudaMemsetAsync(g->indeg.ptr, 0, sizeof(uint32_t) * (size_t)V, g->stream));
+        EG_CUDA(cudaMemsetAsync(g->csr_off.ptr, 0, sizeof(uint64_t) * ((size_t)V + 1), g->stream));
+        EG_CUDA(cudaMemsetAsync(g->csc_off.ptr, 0, sizeof(uint64_t) * ((size_t)V + 1), g->stream));
+        return EG_OK;
+    }
+    const BucketPlan pl = plan_buckets(V, E);
+    const uint64_t ncnt = 2ull * pl.nb * pl.nblk;
+    EG_TRY(g->bucket_cnt.reserve(sizeof(uint32_t) * ncnt));
+    EG_TRY(g->bucket_off.reserve(sizeof(uint64_t) * (ncnt + 1)));
+    EG_TRY(g->bucketed.reserve((size_t)2 * E * rec + 64));
+    EG_TRY(g->scan.counter.reserve(16));
+    {
+        Timed t(&g->prof, g->stream, "bucket_hist");
+        size_t smem = sizeof(uint32_t) * 2 * pl.nb;
+        if (rec == 8) {
+            EG_CUDA(cudaFuncSetAttribute(k_bucket_hist<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_bucket_hist<8><<<pl.nblk, kBucketThreads, smem, g->stream>>>(g->edges.as<uint8_t>(), E, pl.chunk, pl.shift,
+                                                                            pl.nb, pl.nblk, g->bucket_cnt.as<uint32_t>());
+        } else {
+            EG_CUDA(cudaFuncSetAttribute(k_bucket_hist<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_bucket_hist<12><<<pl.nblk, kBucketThreads, smem, g->stream>>>(g->edges.as<uint8_t>(), E, pl.chunk, pl.shift,
+                                                                             pl.nb, pl.nblk, g->bucket_cnt.as<uint32_t>());
+        }
+        EG_CHECK_LAUNCH("k_bucket_hist");
+    }
+    EG_TRY(scan_exclusive_u32(g, g->bucket_cnt.as<uint32_t>(), ncnt, g->bucket_off.as<uint64_t>()));
+    {
+        Timed t(&g->prof, g->stream, "bucket_scatter");
+        size_t smem = sizeof(uint64_t) * 2 * pl.nb + sizeof(uint32_t) * pl.nb + (size_t)kScatterTile * rec;
+        if (rec == 8) {
+            EG_CUDA(cudaFuncSetAttribute(k_bucket_scatter<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_bucket_scatter<8><<<pl.nblk, kScatterThreads, smem, g->stream>>>(
+                g->edges.as<uint8_t>(), E, pl.chunk, pl.shift, pl.nb, pl.nblk, g->bucket_off.as<uint64_t>(),
+                g->bucketed.as<uint8_t>());
+        } else {
+            EG_CUDA(cudaFuncSetAttribute(k_bucket_scatter<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_bucket_scatter<12><<<pl.nblk, kScatterThreads, smem, g->stream>>>(
+                g->edges.as<uint8_t>(), E, pl.chunk, pl.shift, pl.nb, pl.nblk, g->bucket_off.as<uint64_t>(),
+                g->bucketed.as<uint8_t>());
+        }
+        EG_CHECK_LAUNCH("k_bucket_scatter");
+    }
+    const size_t smem_c = sizeof(uint32_t) * pl.LB;
+    for (int half = 0; half < 2; ++half) {
+        EG_CUDA(cudaMemsetAsync(g->scan.counter.ptr, 0, 4, g->stream));
+        Timed t(&g->prof, g->stream, "bucket_build");
+        const uint8_t* recs = g->bucketed.as<uint8_t>() + (size_t)half * E * rec;
+        const uint64_t* ex = g->bucket_off.as<uint64_t>() + (size_t)half * pl.nb * pl.nblk;
+        uint32_t* deg = half == 0 ? g->outdeg.as<uint32_t>() : g->indeg.as<uint32_t>();
+        uint64_t* off = half == 0 ? g->csr_off.as<uint64_t>() : g->csc_off.as<uint64_t>();
+        uint32_t* adj = half == 0 ? g->csr_adj.as<uint32_t>() : g->csc_adj.as<uint32_t>();
+        float* w = half == 0 ? g->csr_w.as<float>() : g->csc_w.as<float>();
+        unsigned grid = std::min<uint32_t>(pl.nb, 152u * 2u);
+        if (rec == 8) {
+            EG_CUDA(cudaFuncSetAttribute(k_bucket_build<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
+            k_bucket_build<8><<<grid, kBuildThreads, smem_c, g->stream>>>(recs, ex, (uint64_t)half * E, E, pl.nb, pl.nblk,
+                                                                          pl.LB, V, half == 0, deg, off, adj, w,
+                                                                          g->scan.counter.as<uint32_t>());
+        } else {
+            EG_CUDA(cudaFuncSetAttribute(k_bucket_build<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
+            k_bucket_build<12><<<grid, kBuildThreads, smem_c, g->stream>>>(recs, ex, (uint64_t)half * E, E, pl.nb, pl.nblk,
+                                                                           pl.LB, V, half == 0, deg, off, adj, w,
+                                                                           g->scan.counter.as<uint32_t>());
+        }
+        EG_CHECK_LAUNCH("k_bucket_build");
+    }
+    return EG_OK;
+}
+
 // ---------------------------------------------------------------------------------------------
 int compute_degrees(eg_graph* g) {
     const uint64_t E = g->E;
@@ -404,7 +734,16 @@ int build_structures(eg_graph* g, int want_csr, int want_csc) {
     g->built_csr = g->built_csc = false;
     g->eng.pull_ready = false;
 
-    EG_TRY(compute_degrees(g));
+    // the bucket tables and a staging tile must fit one CTA's shared memory
+    const bool bucketed =
+        P == 1 && 20ull * plan_buckets(V, E).nb + (uint64_t)kScatterTile * g->edge_bytes <= 200ull * 1024;
+    if (bucketed) {
+        // one partition: both structures (and both degree arrays) from the bucketed build
+        want_csr = want_csc = 1;
+        EG_TRY(build_single(g, 1, 1));
+    } else {
+        EG_TRY(compute_degrees(g));
+    }
     // assign_vertices: dense (out-degree) weights with T = max_iterations
     g->part_off.assign(P + 1, 0);
     g->local_off.assign((size_t)P * (S + 1), 0);
@@ -443,23 +782,23 @@ int build_structures(eg_graph* g, int want_csr, int want_csc) {
         cnt_csr = g->cnt_csr.as<uint32_t>();
         cnt_csc = g->cnt_csc.as<uint32_t>();
     }
-    // offsets: inclusive scans (P == 1: entry V receives the total)
+    // offsets: inclusive scans, then the atomic scatter (generic path, P > 1)
     const size_t off_bytes = sizeof(uint64_t) * (size_t)P * stride;
-    if (want_csr) {
+    if (!bucketed && want_csr) {
         EG_TRY(g->csr_off.reserve(off_bytes));
         EG_TRY(g->csr_adj.reserve(sizeof(uint32_t) * (E + 32)));
         if (g->weighted) EG_TRY(g->csr_w.reserve(sizeof(float) * E));
         EG_TRY(scan_u32_to_u64(g, cnt_csr, n_scan, g->csr_off.as<uint64_t>(),
                                P == 1 ? g->csr_off.as<uint64_t>() + V : nullptr));
     }
-    if (want_csc) {
+    if (!bucketed && want_csc) {
         EG_TRY(g->csc_off.reserve(off_bytes));
         EG_TRY(g->csc_adj.reserve(sizeof(uint32_t) * (E + 32)));
         if (g->weighted) EG_TRY(g->csc_w.reserve(sizeof(float) * E));
         EG_TRY(scan_u32_to_u64(g, cnt_csc, n_scan, g->csc_off.as<uint64_t>(),
                                P == 1 ? g->csc_off.as<uint64_t>() + V : nullptr));
     }
-    if (E) {
+    if (!bucketed && E) {
         Timed t(&g->prof, g->stream, "scatter");
         unsigned grid = grid_for(E, 256, 152u * 16u);
         auto a_off = want_csr ? g->csr_off.as<unsigned long long>() : nullptr;

@@ -102,7 +102,7 @@ struct EngineState {
     DevBuf q0, q1;         // frontier queues (u32 vertex ids)
     DevBuf qdeg;           // u64 prefix of frontier item degrees
     DevBuf chunk_item;     // u32 first item per edge chunk
-    DevBuf bm_visit, bm_next;  // bitmaps (u64 words)
+    DevBuf bm_visit, bm_next, bm_front;  // bitmaps (u64 words)
     DevBuf counters;       // u64 small device counters
     DevBuf acc;            // float / u32 per-vertex accumulator for split items
     DevBuf vals0, vals1;   // per-vertex values
@@ -119,6 +119,7 @@ struct EngineState {
 // the opaque handle of the C ABI
 struct eg_graph {
     int device = 0;
+    int num_sms = 152;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     // construction parameters (Graph(int eta), toolkit flags)
@@ -153,12 +154,16 @@ struct eg_graph {
     eg::ScanScratch scan;
     eg::DevBuf tmp64;  // generic u64 scratch
     eg::DevBuf cpbt_scratch;
+    eg::DevBuf bucket_cnt, bucket_off, bucketed;  // one-partition bucketed build
     eg::DevBuf err;    // device error flags (int)
     eg::EngineState eng;
     eg::Profiler prof;
     // pinned staging for host inputs
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
+    // engine options (eg_set_option)
+    int bfs_direction = 0;  // 0: Gemini threshold switch, 1: push only, 2: pull only
+    int dense_div = 20;     // sparse iff active_edges < E / dense_div (core/graph.hpp:1491)
     // last operator statistics
     uint64_t last_edges_processed = 0;
     int last_iterations = 0;

@@ -52,11 +52,11 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
                                                         const uint64_t* __restrict__ cidx,
                                                         const uint32_t* __restrict__ cvert,
                                                         const uint32_t* __restrict__ chunk_item, uint64_t E,
-                                                        uint64_t nitems, uint64_t nchunks, uint32_t V) {
+                                                        uint64_t nitems, uint64_t nchunks, uint32_t V, int cap) {
     using Acc = typename Op::Acc;
     extern __shared__ __align__(16) unsigned char s_raw[];
-    const int cap = (int)kPullChunk + kMaxPartitions + 2;
-    uint64_t* s_idx = reinterpret_cast<uint64_t*>(s_raw);
+    // item boundaries relative to the chunk start, clamped to [0, chunk]: 4 bytes per item
+    uint32_t* s_idx = reinterpret_cast<uint32_t*>(s_raw);
     Acc* s_acc = reinterpret_cast<Acc*>(s_idx + cap + 1);
     for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const uint64_t e0 = c * kPullChunk;
@@ -65,12 +65,17 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
         const uint32_t j = chunk_item[c + 1];
         const uint32_t iend = (j < nitems && cidx[j] < e1) ? j + 1 : j;
         const int nit = (int)(iend - i0);
+        const bool first_open = cidx[i0] < e0;     // first item began in an earlier chunk
+        const bool last_open = cidx[iend] > e1;    // last item continues into a later chunk
         for (int k = threadIdx.x; k <= nit; k += blockDim.x) {
-            s_idx[k] = cidx[i0 + k];
+            const uint64_t x = cidx[i0 + k];
+            s_idx[k] = x <= e0 ? 0u : (x >= e1 ? (uint32_t)(e1 - e0) : (uint32_t)(x - e0));
             if (k < nit) s_acc[k] = op.identity();
         }
         __syncthreads();
         const uint64_t eb = e0 + (uint64_t)threadIdx.x * kPullPerThread;
+        int fin_key = 0x7fffffff;  // destination of this thread's last (open) segment
+        Acc fin = op.identity();
         if (eb < e1) {
             const uint64_t ee = eb + kPullPerThread < e1 ? eb + kPullPerThread : e1;
             uint32_t ids[kPullPerThread];
@@ -88,19 +93,21 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
             Acc vals[kPullPerThread];
 #pragma unroll
             for (int q = 0; q < kPullPerThread; ++q) vals[q] = eb + q < ee ? op.gather(ids[q], eb + q) : op.identity();
-            // item holding eb: last k with s_idx[k] <= eb
+            // item holding eb: last k with s_idx[k] <= eb - e0
+            const uint32_t rb = (uint32_t)(eb - e0);
             int lo = 0, hi = nit;
             while (hi - lo > 1) {
                 int mid = (lo + hi) >> 1;
-                if (s_idx[mid] <= eb) lo = mid; else hi = mid;
+                if (s_idx[mid] <= rb) lo = mid; else hi = mid;
             }
             int k = lo;
-            uint64_t nb = s_idx[k + 1];
+            uint32_t nb = s_idx[k + 1];
             Acc a = op.identity();
+            const uint32_t re = (uint32_t)(ee - e0);
 #pragma unroll
             for (int q = 0; q < kPullPerThread; ++q) {
-                const uint64_t e = eb + q;
-                if (e < ee) {
+                const uint32_t e = rb + q;
+                if (e < re) {
                     while (e >= nb) {
                         op.smem_add(&s_acc[k], a);
                         a = op.identity();
@@ -110,7 +117,22 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
                     a = op.combine(a, vals[q]);
                 }
             }
-            op.smem_add(&s_acc[k], a);
+            fin_key = k;
+            fin = a;
+        }
+        // the open segments of consecutive threads share destinations (a hub spans whole warps):
+        // segmented inclusive scan over lanes (keys are non-decreasing in lane order), one shared
+        // update per run and warp
+        {
+            const int lane = threadIdx.x & 31;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                Acc vo = __shfl_up_sync(0xffffffffu, fin, o);
+                int ko = __shfl_up_sync(0xffffffffu, fin_key, o);
+                if (lane >= o && ko == fin_key) fin = op.combine(fin, vo);
+            }
+            const int knext = __shfl_down_sync(0xffffffffu, fin_key, 1);
+            if (fin_key != 0x7fffffff && (lane == 31 || knext != fin_key)) op.smem_add(&s_acc[fin_key], fin);
         }
         __syncthreads();
         const int rounds = (nit + (int)blockDim.x - 1) / (int)blockDim.x;
@@ -120,7 +142,7 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
             uint32_t v = ok ? cvert[i0 + k] : V;
             if (v >= V) ok = false;  // partition sentinels
             Acc a = ok ? s_acc[k] : op.identity();
-            bool whole = ok && s_idx[k] >= e0 && s_idx[k + 1] <= e1;
+            bool whole = ok && !(k == 0 && first_open) && !(k == nit - 1 && last_open);
             op.finish(ok, v, a, whole);
         }
         __syncthreads();
@@ -233,6 +255,7 @@ struct EpiItemRank {
 // toolkit operators
 struct BfsOp {  // toolkits/bfs.cpp:52-58: first visitor of dst becomes its parent
     unsigned long long* visited;
+    unsigned long long* next_front;
     uint32_t* level;
     uint32_t* parent;
     uint32_t next_level;
@@ -244,9 +267,47 @@ struct BfsOp {  // toolkits/bfs.cpp:52-58: first visitor of dst becomes its pare
         if (atomicOr(word, bit) & bit) return false;
         if (level) level[w] = next_level;
         if (parent) parent[w] = u;
+        atomicOr(next_front + (w >> 6), bit);
         return true;
     }
 };
+
+// dense BFS step (toolkits/bfs.cpp:60-76): every unvisited destination looks for any in-neighbour
+// in the current frontier and stops at the first one; the winner of the visited bit activates it
+__global__ void __launch_bounds__(256) k_bfs_pull(const uint32_t* __restrict__ cvert, const uint64_t* __restrict__ cidx,
+                                                   uint64_t nitems, const uint32_t* __restrict__ adj,
+                                                   const unsigned long long* __restrict__ front,
+                                                   unsigned long long* visited, unsigned long long* next_front,
+                                                   uint32_t* level, uint32_t* parent, uint32_t next_level,
+                                                   uint32_t* q_out, uint32_t* n_out, unsigned long long* act_edges,
+                                                   const uint32_t* __restrict__ deg, uint32_t V) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nitems; base += stride) {
+        const uint64_t i = base + threadIdx.x;
+        bool act = false;
+        uint32_t v = V;
+        if (i < nitems) {
+            v = cvert[i];
+            if (v < V && !((__ldcg(visited + (v >> 6)) >> (v & 63)) & 1ull)) {
+                const uint64_t e1 = cidx[i + 1];
+                for (uint64_t e = cidx[i]; e < e1; ++e) {
+                    const uint32_t u = __ldg(adj + e);
+                    if ((__ldg(front + (u >> 6)) >> (u & 63)) & 1ull) {
+                        const unsigned long long bit = 1ull << (v & 63);
+                        if (!(atomicOr(visited + (v >> 6), bit) & bit)) {
+                            if (level) level[v] = next_level;
+                            if (parent) parent[v] = u;
+                            atomicOr(next_front + (v >> 6), bit);
+                            act = true;
+                        }
+                        break;
+                    }
+                }
+            }
+        }
+        append_active(act, v, q_out, n_out, act_edges, deg);
+    }
+}
 
 struct SsspOp {  // toolkits/sssp.cpp:52-64: relax_dist = dist[src] + w; write_min
     float* dist;
@@ -383,10 +444,12 @@ __global__ void k_pr_finish_all(const uint32_t* __restrict__ indeg, uint32_t V, 
         next[v] = x;
     }
 }
-__global__ void k_bfs_root(uint32_t* level, uint32_t* parent, unsigned long long* visited, uint32_t root, uint32_t* q) {
+__global__ void k_bfs_root(uint32_t* level, uint32_t* parent, unsigned long long* visited, unsigned long long* front,
+                           uint32_t root, uint32_t* q) {
     if (level) level[root] = 0;
     if (parent) parent[root] = root;
     visited[root >> 6] |= 1ull << (root & 63);
+    front[root >> 6] |= 1ull << (root & 63);
     q[0] = root;
 }
 __global__ void k_sssp_root(float* dist, uint32_t root, uint32_t* q) {
@@ -427,14 +490,17 @@ static int launch_pull(eg_graph* g, const Op& op, const char* name) {
     EngineState& s = g->eng;
     const uint64_t nitems = g->ncompressed - 1;
     if (s.pull_nchunks == 0) return EG_OK;
-    const size_t cap = kPullChunk + kMaxPartitions + 2;
-    const size_t smem = sizeof(uint64_t) * (cap + 1) + sizeof(typename Op::Acc) * cap;
+    // a chunk holds at most one item per edge plus the zero-length sentinels of empty partitions
+    const int cap = (int)kPullChunk + g->partitions + 2;
+    const size_t smem = sizeof(uint32_t) * (cap + 1) + sizeof(typename Op::Acc) * cap;
     EG_CUDA(cudaFuncSetAttribute(k_pull<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    unsigned grid = (unsigned)std::min<uint64_t>(s.pull_nchunks, 152ull * 4ull);
+    int per_sm = 0;
+    EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<Op>, kPullThreads, smem));
+    unsigned grid = (unsigned)std::min<uint64_t>(s.pull_nchunks, (uint64_t)g->num_sms * (uint64_t)std::max(per_sm, 1));
     Timed t(&g->prof, g->stream, name);
     k_pull<Op><<<grid, kPullThreads, smem, g->stream>>>(op, g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(),
                                                         g->cvert.as<uint32_t>(), s.pull_chunk_item.as<uint32_t>(), g->E,
-                                                        nitems, s.pull_nchunks, g->V);
+                                                        nitems, s.pull_nchunks, g->V, cap);
     EG_CHECK_LAUNCH(name);
     return EG_OK;
 }
@@ -449,6 +515,7 @@ static int ensure_engine(eg_graph* g) {
     EG_TRY(s.chunk_item.reserve(sizeof(uint32_t) * (g->E / kPushChunk + 4)));
     EG_TRY(s.bm_visit.reserve(sizeof(uint64_t) * (V / 64 + 1)));
     EG_TRY(s.bm_next.reserve(sizeof(uint64_t) * (V / 64 + 1)));
+    EG_TRY(s.bm_front.reserve(sizeof(uint64_t) * (V / 64 + 1)));
     EG_TRY(s.counters.reserve(64));
     EG_TRY(s.acc.reserve(sizeof(float) * (V + 1)));
     EG_TRY(s.vals0.reserve(sizeof(float) * (V + 1)));
@@ -575,24 +642,67 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
     uint32_t* d_level = s.vals0.as<uint32_t>();
     uint32_t* d_parent = s.vals1.as<uint32_t>();
     const unsigned gv = grid_for(V, 256, 152u * 16u);
+    const size_t bm_bytes = sizeof(uint64_t) * (V / 64 + 1);
+    unsigned long long* front = s.bm_next.as<unsigned long long>();
+    unsigned long long* next_front = s.bm_front.as<unsigned long long>();
     {
         Timed t(&g->prof, g->stream, "bfs_init");
         k_fill_u32<<<gv, 256, 0, g->stream>>>(d_level, V, 0xFFFFFFFFu);
         k_fill_u32<<<gv, 256, 0, g->stream>>>(d_parent, V, V);
-        EG_CUDA(cudaMemsetAsync(s.bm_visit.ptr, 0, sizeof(uint64_t) * (V / 64 + 1), g->stream));
-        k_bfs_root<<<1, 1, 0, g->stream>>>(d_level, d_parent, s.bm_visit.as<unsigned long long>(), root, s.q0.as<uint32_t>());
+        EG_CUDA(cudaMemsetAsync(s.bm_visit.ptr, 0, bm_bytes, g->stream));
+        EG_CUDA(cudaMemsetAsync(front, 0, bm_bytes, g->stream));
+        EG_CUDA(cudaMemsetAsync(next_front, 0, bm_bytes, g->stream));
+        k_bfs_root<<<1, 1, 0, g->stream>>>(d_level, d_parent, s.bm_visit.as<unsigned long long>(), front, root,
+                                           s.q0.as<uint32_t>());
         EG_CHECK_LAUNCH("k_bfs_root");
     }
+    uint32_t root_deg = 0;
+    EG_CUDA(cudaMemcpyAsync(&root_deg, g->outdeg.as<uint32_t>() + root, 4, cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
     uint32_t* qa = s.q0.as<uint32_t>();
     uint32_t* qb = s.q1.as<uint32_t>();
-    uint64_t n = 1, total_edges = 0, reach = 1;
+    uint64_t n = 1, reach = 1;
+    unsigned long long active_edges = root_deg, total_edges = root_deg;
     uint32_t lvl = 0;
+    int pushes = 0, pulls = 0;
+    const uint64_t nitems = g->built_csc ? g->ncompressed - 1 : 0;
     while (n > 0) {
-        BfsOp op{s.bm_visit.as<unsigned long long>(), d_level, d_parent, lvl + 1};
+        // core/graph.hpp:1484-1491 (Gemini's switch): sparse iff the frontier's out-edges < E / div
+        const bool dense = g->bfs_direction == 2 ||
+                           (g->bfs_direction == 0 && g->built_csc && active_edges >= g->E / (uint64_t)g->dense_div);
         uint32_t nout = 0;
-        uint64_t T = 0;
-        EG_TRY(push_level(g, op, qa, n, qb, &nout, &T, nullptr, nullptr, "bfs_push"));
-        total_edges += T;
+        unsigned long long act = 0;
+        if (!dense) {
+            BfsOp op{s.bm_visit.as<unsigned long long>(), next_front, d_level, d_parent, lvl + 1};
+            EG_TRY(push_level(g, op, qa, n, qb, &nout, nullptr, &act, g->outdeg.as<uint32_t>(), "bfs_push"));
+            ++pushes;
+        } else {
+            uint32_t* d_nout = reinterpret_cast<uint32_t*>(s.counters.as<unsigned long long>() + 2);
+            unsigned long long* d_act = s.counters.as<unsigned long long>() + 3;
+            EG_CUDA(cudaMemsetAsync(d_nout, 0, 16, g->stream));
+            {
+                Timed t(&g->prof, g->stream, "bfs_pull");
+                k_bfs_pull<<<grid_for(nitems, 256, 152u * 16u), 256, 0, g->stream>>>(
+                    g->cvert.as<uint32_t>(), g->cidx.as<uint64_t>(), nitems, g->csc_adj.as<uint32_t>(), front,
+                    s.bm_visit.as<unsigned long long>(), next_front, d_level, d_parent, lvl + 1, qb, d_nout, d_act,
+                    g->outdeg.as<uint32_t>(), V);
+                EG_CHECK_LAUNCH("k_bfs_pull");
+            }
+            struct {
+                uint32_t n;
+                uint32_t pad;
+                unsigned long long act;
+            } h;
+            EG_CUDA(cudaMemcpyAsync(&h, d_nout, 16, cudaMemcpyDeviceToHost, g->stream));
+            EG_CUDA(cudaStreamSynchronize(g->stream));
+            nout = h.n;
+            act = h.act;
+            ++pulls;
+        }
+        EG_CUDA(cudaMemsetAsync(front, 0, bm_bytes, g->stream));
+        std::swap(front, next_front);
+        total_edges += act;
+        active_edges = act;
         reach += nout;
         std::swap(qa, qb);
         n = nout;
@@ -602,10 +712,10 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
     EG_TRY(copy_out(g, parent, d_parent, sizeof(uint32_t) * (size_t)V, where));
     EG_CUDA(cudaStreamSynchronize(g->stream));
     if (reached) *reached = reach;
-    g->last_edges_processed = total_edges;
+    g->last_edges_processed = total_edges;  // sum of out-degrees of the reached vertices
     g->last_iterations = (int)lvl;
-    g->last_pushes = (int)lvl;
-    g->last_pulls = 0;
+    g->last_pushes = pushes;
+    g->last_pulls = pulls;
     return EG_OK;
 }
 
@@ -677,7 +787,7 @@ int run_cc(eg_graph* g, uint32_t* label, int where) {
         uint32_t nout = 0;
         unsigned long long act = 0;
         // core/graph.hpp:1484-1491: sparse iff active_edges < edges / 20
-        const bool sparse = active_edges < g->E / 20;
+        const bool sparse = active_edges < g->E / (uint64_t)g->dense_div;
         if (sparse) {
             CcPushOp op{d_label, s.bm_next.as<unsigned long long>()};
             uint64_t T = 0;

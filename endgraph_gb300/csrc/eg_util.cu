@@ -125,6 +125,16 @@ int scan_u32_to_u64(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out_i
     return launch_scan(g, LoadU32{in}, EpiInclusive{out_incl}, n, total_dev, "scan_offsets");
 }
 
+struct EpiExclusive {
+    uint64_t* out;
+    __device__ void operator()(uint64_t i, uint64_t excl, uint32_t) const { out[i] = excl; }
+};
+
+// out[i] = sum(in[0..i)), out[n] = total
+int scan_exclusive_u32(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out) {
+    return launch_scan(g, LoadU32{in}, EpiExclusive{out}, n, out + n, "scan_buckets");
+}
+
 // ---------------------------------------------------------------------------------------------
 // compressed incoming index (core/graph.hpp:1144-1188): one (vertex, start) per non-empty list
 // (p, v) plus a sentinel (V, partition end) per partition; cnt holds P*(V+1) counts with the

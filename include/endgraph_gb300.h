@@ -146,6 +146,14 @@ int eg_cc(eg_graph* g, uint32_t* label, int where);
 /* SSSP (toolkits/sssp.cpp:24-84), push Bellman-Ford on float weights; unreached = 1e9. */
 int eg_sssp(eg_graph* g, uint32_t root, float* dist, int where);
 
+/* Engine options.  EG_OPT_DENSE_DIVISOR: process_edges runs sparse (push) iff the active
+ * vertices' out-edges < E / divisor (core/graph.hpp:1484-1491; the reference uses 20).
+ * EG_OPT_BFS_DIRECTION: 0 applies that switch to BFS with the toolkit's dense callbacks
+ * (toolkits/bfs.cpp:60-76), 1 forces push every level as the reference's use_root flag does
+ * (core/graph.hpp:1496-1498), 2 forces pull.  Results are identical in every mode. */
+enum { EG_OPT_BFS_DIRECTION = 1, EG_OPT_DENSE_DIVISOR = 2 };
+int eg_set_option(eg_graph* g, int option, int64_t value);
+
 /* statistics of the last toolkit call: edges traversed, iterations, push / pull iterations */
 int eg_last_run(eg_graph* g, uint64_t* edges_processed, int* iterations, int* push_iters, int* pull_iters);
 

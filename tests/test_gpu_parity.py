@@ -95,6 +95,31 @@ def test_bfs(eg_lib, V, E, seed, P):
             assert oracle.bfs_check_parents(csr["off"][0], csr["adj"], V, root, lv, par) == 0
 
 
+@pytest.mark.parametrize("direction", [0, 1, 2])
+@pytest.mark.parametrize("P", [1, 2])
+def test_bfs_directions(eg_lib, direction, P):
+    """Push-only (the reference's use_root mode), pull-only and Gemini's switch give the same levels."""
+    import endgraph_gb300 as eg
+    V, E = 1 << 16, 1 << 20
+    src, dst, _ = rmat_graph(V, E, 77)
+    csr = oracle.build_csr(src, dst, None, V, np.array([0, V], np.uint32))
+    with _graph(eg_lib, P=P) as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        g.set_option(eg.EG_OPT_BFS_DIRECTION, direction)
+        for root in [int(src[3]), int(dst[5])]:
+            lv_ref = oracle.bfs_levels(csr["off"][0], csr["adj"], V, root)
+            lv, par = g.bfs(root)
+            assert np.array_equal(lv, lv_ref)
+            assert oracle.bfs_check_parents(csr["off"][0], csr["adj"], V, root, lv, par) == 0
+            run = g.last_run()
+            reach_edges = int(np.asarray(np.diff(csr["off"][0].astype(np.int64)))[lv_ref != oracle.UNREACHED].sum())
+            assert run["edges"] == reach_edges
+            if direction == 1:
+                assert run["pull"] == 0
+            if direction == 2:
+                assert run["push"] == 0
+
+
 @pytest.mark.parametrize("V,E,seed", CASES)
 def test_cc(eg_lib, V, E, seed):
     import endgraph_gb300 as eg
