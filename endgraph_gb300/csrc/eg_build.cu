@@ -295,7 +295,8 @@ __global__ void k_part_edges(const uint64_t* off, uint32_t V, int P, uint64_t E,
 // =============================================================================================
 constexpr int kBucketThreads = 512;
 constexpr int kBuildThreads = 1024;
-constexpr uint32_t kMaxBucketVerts = 16384;
+constexpr uint32_t kMaxBucketVerts = 32768;  // 128 KiB of shared-memory counters in pass C
+constexpr int kBuildUnroll = 4;
 
 template <int REC>
 __global__ void __launch_bounds__(kBucketThreads) k_bucket_hist(const uint8_t* __restrict__ edges, uint64_t E,
@@ -457,6 +458,50 @@ __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_
     }
 }
 
+// Visit records [r0, r1) of a bucket with several loads in flight per thread.  8-byte records go
+// as 16-byte pairs when the buffer is 16-byte aligned (vec); a pair straddling r0 or r1 visits
+// only its in-range half.
+template <int REC, class F>
+__device__ __forceinline__ void for_records(const uint8_t* __restrict__ rec, uint64_t r0, uint64_t r1, bool vec, F f) {
+    if (REC == 8 && vec) {
+        const uint4* p = reinterpret_cast<const uint4*>(rec);
+        const uint64_t q1 = (r1 + 1) / 2;
+        for (uint64_t q = r0 / 2 + threadIdx.x; q < q1; q += (uint64_t)blockDim.x * kBuildUnroll) {
+            uint4 x[kBuildUnroll];
+#pragma unroll
+            for (int u = 0; u < kBuildUnroll; ++u) {
+                const uint64_t qq = q + (uint64_t)u * blockDim.x;
+                if (qq < q1) x[u] = __ldcs(p + qq);
+            }
+#pragma unroll
+            for (int u = 0; u < kBuildUnroll; ++u) {
+                const uint64_t r = 2 * (q + (uint64_t)u * blockDim.x);
+                if (r < 2 * q1) {
+                    if (r >= r0) f(x[u].x, x[u].y, 0u);
+                    if (r + 1 < r1) f(x[u].z, x[u].w, 0u);
+                }
+            }
+        }
+    } else {
+        for (uint64_t r = r0 + threadIdx.x; r < r1; r += (uint64_t)blockDim.x * kBuildUnroll) {
+            uint32_t s[kBuildUnroll], d[kBuildUnroll], w[kBuildUnroll];
+#pragma unroll
+            for (int u = 0; u < kBuildUnroll; ++u) {
+                const uint64_t ru = r + (uint64_t)u * blockDim.x;
+                if (ru < r1) {
+                    const uint32_t* p = reinterpret_cast<const uint32_t*>(rec + ru * REC);
+                    s[u] = __ldcs(p);
+                    d[u] = __ldcs(p + 1);
+                    w[u] = REC == 12 ? __ldcs(p + 2) : 0u;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kBuildUnroll; ++u)
+                if (r + (uint64_t)u * blockDim.x < r1) f(s[u], d[u], w[u]);
+        }
+    }
+}
+
 // C: one bucket per CTA iteration (persistent CTAs take buckets from a ticket)
 template <int REC>
 __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* __restrict__ rec, const uint64_t* __restrict__ excl,
@@ -464,7 +509,8 @@ __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* _
                                                                  uint32_t LB, uint32_t V, int key_is_src,
                                                                  uint32_t* __restrict__ deg, uint64_t* __restrict__ off,
                                                                  uint32_t* __restrict__ adj, float* __restrict__ wout,
-                                                                 uint32_t* ticket) {
+                                                                 uint32_t* ticket, int vec_ok) {
+    const bool vec = vec_ok != 0;
     extern __shared__ uint32_t s_cnt[];  // LB counters
     __shared__ uint32_t s_warp[32];
     __shared__ uint32_t s_b;
@@ -479,11 +525,9 @@ __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* _
         const uint64_t r1 = b + 1 < nb ? excl[(uint64_t)(b + 1) * nblk] - half_base : E;
         for (uint32_t i = threadIdx.x; i < nv; i += blockDim.x) s_cnt[i] = 0;
         __syncthreads();
-        for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-            const uint32_t* p = reinterpret_cast<const uint32_t*>(rec + r * REC);
-            const uint32_t key = (key_is_src ? p[0] : p[1]) - v0;
-            atomicAdd(&s_cnt[key], 1u);
-        }
+        for_records<REC>(rec, r0, r1, vec, [&](uint32_t s, uint32_t d, uint32_t) {
+            atomicAdd(&s_cnt[(key_is_src ? s : d) - v0], 1u);
+        });
         __syncthreads();
         // degrees out, then offsets from the block scan
         for (uint32_t i = threadIdx.x; i < nv; i += blockDim.x) deg[v0 + i] = s_cnt[i];
@@ -492,14 +536,11 @@ __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* _
         for (uint32_t i = threadIdx.x; i < nv; i += blockDim.x) off[v0 + i] = r0 + s_cnt[i];
         if (threadIdx.x == 0 && v0 + nv == V) off[V] = r1;
         __syncthreads();
-        for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-            const uint32_t* p = reinterpret_cast<const uint32_t*>(rec + r * REC);
-            const uint32_t s = p[0], d = p[1];
-            const uint32_t key = (key_is_src ? s : d) - v0;
-            const uint64_t pos = r0 + atomicAdd(&s_cnt[key], 1u);
+        for_records<REC>(rec, r0, r1, vec, [&](uint32_t s, uint32_t d, uint32_t wb) {
+            const uint64_t pos = r0 + atomicAdd(&s_cnt[(key_is_src ? s : d) - v0], 1u);
             adj[pos] = key_is_src ? d : s;
-            if (REC == 12) wout[pos] = __uint_as_float(p[2]);
-        }
+            if (REC == 12) wout[pos] = __uint_as_float(wb);
+        });
         __syncthreads();
     }
 }
@@ -587,6 +628,8 @@ static int build_single(eg_graph* g, int want_csr, int want_csc) {
         EG_CHECK_LAUNCH("k_bucket_scatter");
     }
     const size_t smem_c = sizeof(uint32_t) * pl.LB;
+    if (rec == 8) EG_CUDA(cudaFuncSetAttribute(k_bucket_build<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
+    else EG_CUDA(cudaFuncSetAttribute(k_bucket_build<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
     for (int half = 0; half < 2; ++half) {
         EG_CUDA(cudaMemsetAsync(g->scan.counter.ptr, 0, 4, g->stream));
         Timed t(&g->prof, g->stream, "bucket_build");
@@ -596,17 +639,21 @@ static int build_single(eg_graph* g, int want_csr, int want_csc) {
         uint64_t* off = half == 0 ? g->csr_off.as<uint64_t>() : g->csc_off.as<uint64_t>();
         uint32_t* adj = half == 0 ? g->csr_adj.as<uint32_t>() : g->csc_adj.as<uint32_t>();
         float* w = half == 0 ? g->csr_w.as<float>() : g->csc_w.as<float>();
-        unsigned grid = std::min<uint32_t>(pl.nb, 152u * 2u);
+        int per_sm = 1;
+        if (rec == 8)
+            EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bucket_build<8>, kBuildThreads, smem_c));
+        else
+            EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bucket_build<12>, kBuildThreads, smem_c));
+        unsigned grid = std::min<uint32_t>(pl.nb, (uint32_t)g->num_sms * (uint32_t)std::max(per_sm, 1));
         if (rec == 8) {
-            EG_CUDA(cudaFuncSetAttribute(k_bucket_build<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
             k_bucket_build<8><<<grid, kBuildThreads, smem_c, g->stream>>>(recs, ex, (uint64_t)half * E, E, pl.nb, pl.nblk,
                                                                           pl.LB, V, half == 0, deg, off, adj, w,
-                                                                          g->scan.counter.as<uint32_t>());
+                                                                          g->scan.counter.as<uint32_t>(),
+                                                                          ((uintptr_t)recs & 15u) == 0);
         } else {
-            EG_CUDA(cudaFuncSetAttribute(k_bucket_build<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
             k_bucket_build<12><<<grid, kBuildThreads, smem_c, g->stream>>>(recs, ex, (uint64_t)half * E, E, pl.nb, pl.nblk,
                                                                            pl.LB, V, half == 0, deg, off, adj, w,
-                                                                           g->scan.counter.as<uint32_t>());
+                                                                           g->scan.counter.as<uint32_t>(), 0);
         }
         EG_CHECK_LAUNCH("k_bucket_build");
     }

@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
     // item boundaries relative to the chunk start, clamped to [0, chunk]: 4 bytes per item
     uint32_t* s_idx = reinterpret_cast<uint32_t*>(s_raw);
     Acc* s_acc = reinterpret_cast<Acc*>(s_idx + cap + 1);
+    uint8_t* s_on = reinterpret_cast<uint8_t*>(s_acc + cap);  // per-item filter (Op::kFilter)
     for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const uint64_t e0 = c * kPullChunk;
         const uint64_t e1 = e0 + kPullChunk < E ? e0 + kPullChunk : E;
@@ -70,13 +71,46 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
         for (int k = threadIdx.x; k <= nit; k += blockDim.x) {
             const uint64_t x = cidx[i0 + k];
             s_idx[k] = x <= e0 ? 0u : (x >= e1 ? (uint32_t)(e1 - e0) : (uint32_t)(x - e0));
-            if (k < nit) s_acc[k] = op.identity();
+            if (k < nit) {
+                s_acc[k] = op.identity();
+                if (Op::kFilter) {
+                    const uint32_t v = cvert[i0 + k];
+                    s_on[k] = v < V && op.item_active(v);
+                }
+            }
         }
         __syncthreads();
         const uint64_t eb = e0 + (uint64_t)threadIdx.x * kPullPerThread;
         int fin_key = 0x7fffffff;  // destination of this thread's last (open) segment
         Acc fin = op.identity();
+        // item holding eb: last k with s_idx[k] <= eb - e0
+        const uint32_t rb = (uint32_t)(eb - e0);
+        int k0 = 0;
+        uint32_t act = 0;  // edges of this thread whose destination passes the filter
         if (eb < e1) {
+            int lo = 0, hi = nit;
+            while (hi - lo > 1) {
+                int mid = (lo + hi) >> 1;
+                if (s_idx[mid] <= rb) lo = mid; else hi = mid;
+            }
+            k0 = lo;
+            const uint32_t re = (uint32_t)((eb + kPullPerThread < e1 ? eb + kPullPerThread : e1) - e0);
+            if (Op::kFilter) {
+                int k = k0;
+                uint32_t nb = s_idx[k + 1];
+#pragma unroll
+                for (int q = 0; q < kPullPerThread; ++q) {
+                    const uint32_t e = rb + q;
+                    if (e < re) {
+                        while (e >= nb) nb = s_idx[++k + 1];
+                        if (s_on[k]) act |= 1u << q;
+                    }
+                }
+            } else {
+                act = re - rb >= 32 ? 0xFFFFFFFFu : ((1u << (re - rb)) - 1u);
+            }
+        }
+        if (act) {
             const uint64_t ee = eb + kPullPerThread < e1 ? eb + kPullPerThread : e1;
             uint32_t ids[kPullPerThread];
             if (ee - eb == kPullPerThread) {
@@ -92,15 +126,8 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
             }
             Acc vals[kPullPerThread];
 #pragma unroll
-            for (int q = 0; q < kPullPerThread; ++q) vals[q] = eb + q < ee ? op.gather(ids[q], eb + q) : op.identity();
-            // item holding eb: last k with s_idx[k] <= eb - e0
-            const uint32_t rb = (uint32_t)(eb - e0);
-            int lo = 0, hi = nit;
-            while (hi - lo > 1) {
-                int mid = (lo + hi) >> 1;
-                if (s_idx[mid] <= rb) lo = mid; else hi = mid;
-            }
-            int k = lo;
+            for (int q = 0; q < kPullPerThread; ++q) vals[q] = (act >> q) & 1u ? op.gather(ids[q], eb + q) : op.identity();
+            int k = k0;
             uint32_t nb = s_idx[k + 1];
             Acc a = op.identity();
             const uint32_t re = (uint32_t)(ee - e0);
@@ -272,42 +299,45 @@ struct BfsOp {  // toolkits/bfs.cpp:52-58: first visitor of dst becomes its pare
     }
 };
 
-// dense BFS step (toolkits/bfs.cpp:60-76): every unvisited destination looks for any in-neighbour
-// in the current frontier and stops at the first one; the winner of the visited bit activates it
-__global__ void __launch_bounds__(256) k_bfs_pull(const uint32_t* __restrict__ cvert, const uint64_t* __restrict__ cidx,
-                                                   uint64_t nitems, const uint32_t* __restrict__ adj,
-                                                   const unsigned long long* __restrict__ front,
-                                                   unsigned long long* visited, unsigned long long* next_front,
-                                                   uint32_t* level, uint32_t* parent, uint32_t next_level,
-                                                   uint32_t* q_out, uint32_t* n_out, unsigned long long* act_edges,
-                                                   const uint32_t* __restrict__ deg, uint32_t V) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nitems; base += stride) {
-        const uint64_t i = base + threadIdx.x;
+// dense BFS step (toolkits/bfs.cpp:60-76): an unvisited destination takes an in-neighbour that is
+// in the current frontier as its parent (here the smallest one seen by a chunk); destinations that
+// are already visited are filtered out before their in-lists are read
+struct BfsPullOp {
+    using Acc = uint32_t;
+    static constexpr bool kFilter = true;
+    const unsigned long long* front;
+    unsigned long long* visited;
+    unsigned long long* next_front;
+    uint32_t* level;
+    uint32_t* parent;
+    uint32_t next_level;
+    uint32_t* q_out;
+    uint32_t* n_out;
+    unsigned long long* act_edges;
+    const uint32_t* deg;
+    __device__ bool item_active(uint32_t v) const { return !((__ldcg(visited + (v >> 6)) >> (v & 63)) & 1ull); }
+    __device__ Acc identity() const { return 0xFFFFFFFFu; }
+    __device__ Acc gather(uint32_t u, uint64_t) const {
+        return ((__ldg(front + (u >> 6)) >> (u & 63)) & 1ull) ? u : 0xFFFFFFFFu;
+    }
+    __device__ Acc combine(Acc a, Acc b) const { return a < b ? a : b; }
+    __device__ void smem_add(Acc* slot, Acc v) const {
+        if (v != 0xFFFFFFFFu) atomicMin(slot, v);
+    }
+    __device__ void finish(bool ok, uint32_t v, Acc m, bool) const {
         bool act = false;
-        uint32_t v = V;
-        if (i < nitems) {
-            v = cvert[i];
-            if (v < V && !((__ldcg(visited + (v >> 6)) >> (v & 63)) & 1ull)) {
-                const uint64_t e1 = cidx[i + 1];
-                for (uint64_t e = cidx[i]; e < e1; ++e) {
-                    const uint32_t u = __ldg(adj + e);
-                    if ((__ldg(front + (u >> 6)) >> (u & 63)) & 1ull) {
-                        const unsigned long long bit = 1ull << (v & 63);
-                        if (!(atomicOr(visited + (v >> 6), bit) & bit)) {
-                            if (level) level[v] = next_level;
-                            if (parent) parent[v] = u;
-                            atomicOr(next_front + (v >> 6), bit);
-                            act = true;
-                        }
-                        break;
-                    }
-                }
+        if (ok && m != 0xFFFFFFFFu) {
+            const unsigned long long bit = 1ull << (v & 63);
+            if (!(atomicOr(visited + (v >> 6), bit) & bit)) {
+                if (level) level[v] = next_level;
+                if (parent) parent[v] = m;
+                atomicOr(next_front + (v >> 6), bit);
+                act = true;
             }
         }
         append_active(act, v, q_out, n_out, act_edges, deg);
     }
-}
+};
 
 struct SsspOp {  // toolkits/sssp.cpp:52-64: relax_dist = dist[src] + w; write_min
     float* dist;
@@ -339,6 +369,8 @@ struct CcPushOp {  // toolkits/cc.cpp:50-60: msg = label[src]; write_min(label[d
 
 struct PrPullOp {  // toolkits/pagerank.cpp:64-97: sum curr[src]; next = 1-d+d*sum (/ outdeg)
     using Acc = float;
+    static constexpr bool kFilter = false;
+    __device__ bool item_active(uint32_t) const { return true; }
     const float* curr;
     float* next;
     float* acc;
@@ -346,7 +378,7 @@ struct PrPullOp {  // toolkits/pagerank.cpp:64-97: sum curr[src]; next = 1-d+d*s
     float base, d;
     int divide, single;
     __device__ Acc identity() const { return 0.f; }
-    __device__ Acc gather(uint32_t src, uint64_t) const { return __ldg(curr + src); }
+    __device__ Acc gather(uint32_t src, uint64_t) const { return __ldcg(curr + src); }
     __device__ Acc combine(Acc a, Acc b) const { return a + b; }
     __device__ void smem_add(Acc* slot, Acc v) const { atomicAdd(slot, v); }
     __device__ void finish(bool ok, uint32_t v, Acc a, bool whole) const {
@@ -366,6 +398,8 @@ struct PrPullOp {  // toolkits/pagerank.cpp:64-97: sum curr[src]; next = 1-d+d*s
 
 struct CcPullOp {  // toolkits/cc.cpp:62-80: min label over in-neighbours, write_min + activate
     using Acc = uint32_t;
+    static constexpr bool kFilter = false;
+    __device__ bool item_active(uint32_t) const { return true; }
     uint32_t* label;
     unsigned long long* next_bm;
     uint32_t* q_out;
@@ -492,7 +526,7 @@ static int launch_pull(eg_graph* g, const Op& op, const char* name) {
     if (s.pull_nchunks == 0) return EG_OK;
     // a chunk holds at most one item per edge plus the zero-length sentinels of empty partitions
     const int cap = (int)kPullChunk + g->partitions + 2;
-    const size_t smem = sizeof(uint32_t) * (cap + 1) + sizeof(typename Op::Acc) * cap;
+    const size_t smem = sizeof(uint32_t) * (cap + 1) + sizeof(typename Op::Acc) * cap + (Op::kFilter ? cap : 0);
     EG_CUDA(cudaFuncSetAttribute(k_pull<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<Op>, kPullThreads, smem));
@@ -665,7 +699,7 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
     unsigned long long active_edges = root_deg, total_edges = root_deg;
     uint32_t lvl = 0;
     int pushes = 0, pulls = 0;
-    const uint64_t nitems = g->built_csc ? g->ncompressed - 1 : 0;
+    if (g->built_csc) EG_TRY(setup_pull(g));
     while (n > 0) {
         // core/graph.hpp:1484-1491 (Gemini's switch): sparse iff the frontier's out-edges < E / div
         const bool dense = g->bfs_direction == 2 ||
@@ -680,14 +714,9 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
             uint32_t* d_nout = reinterpret_cast<uint32_t*>(s.counters.as<unsigned long long>() + 2);
             unsigned long long* d_act = s.counters.as<unsigned long long>() + 3;
             EG_CUDA(cudaMemsetAsync(d_nout, 0, 16, g->stream));
-            {
-                Timed t(&g->prof, g->stream, "bfs_pull");
-                k_bfs_pull<<<grid_for(nitems, 256, 152u * 16u), 256, 0, g->stream>>>(
-                    g->cvert.as<uint32_t>(), g->cidx.as<uint64_t>(), nitems, g->csc_adj.as<uint32_t>(), front,
-                    s.bm_visit.as<unsigned long long>(), next_front, d_level, d_parent, lvl + 1, qb, d_nout, d_act,
-                    g->outdeg.as<uint32_t>(), V);
-                EG_CHECK_LAUNCH("k_bfs_pull");
-            }
+            BfsPullOp op{front, s.bm_visit.as<unsigned long long>(), next_front, d_level, d_parent, lvl + 1, qb, d_nout,
+                         d_act, g->outdeg.as<uint32_t>()};
+            EG_TRY(launch_pull(g, op, "bfs_pull"));
             struct {
                 uint32_t n;
                 uint32_t pad;

@@ -80,6 +80,35 @@ Graph<E>* make_graph(const uint32_t* src, const uint32_t* dst, const float* w, u
     return g;
 }
 
+// prepare_pull_mode sizes the per-thread dense chunks (tuned_chunks_dense) from `new ULLONG[length]`
+// that it never zeroes before `a[cnt] += eta` (core/graph.hpp:1191-1237).  With non-zero heap
+// contents the u64 prefix inside optimal_offset can wrap, the chunks then overlap and destinations
+// are signalled twice.  Recompute them the way the code evidently intends (a[i] = 0 + eta), which
+// is what the reference computes whenever its heap happens to be zeroed.
+template <typename E>
+void fix_dense_chunks(Graph<E>* g) {
+    for (int i = 0; i < g->partitions_num; ++i) {
+        for (int s_i = 0; s_i < g->sockets_num; ++s_i) {
+            const UINT n = g->compressed_incoming_adj_vertices[s_i];
+            const CompressedAdjIndexType* idx = g->compressed_incoming_adj_index[s_i];
+            UINT p = 0;
+            while (p < n && idx[p].vertex < g->partition_offset[i]) p++;
+            const UINT last = p;
+            while (p < n && idx[p].vertex < g->partition_offset[i + 1]) p++;
+            const UINT length = p - last;
+            std::vector<ULLONG> a(length + 1, (ULLONG)g->eta);
+            UINT* off = g->optimal_offset(a.data(), length, g->threads_per_socket);
+            for (int s_j = 0; s_j < g->threads_per_socket; ++s_j) {
+                ThreadState& ts = g->tuned_chunks_dense[i][s_i * g->threads_per_socket + s_j];
+                ts.status = WORKING;
+                ts.curr = last + off[s_j];
+                ts.end = last + off[s_j + 1];
+            }
+            delete[] off;
+        }
+    }
+}
+
 template <typename E>
 double build(Graph<E>* g) {
     double t = -MPI_Wtime();
@@ -92,6 +121,7 @@ double build(Graph<E>* g) {
                          [](EdgeType<E> e) { return e.src; });
     g->prepare_pull_mode();
     t += MPI_Wtime();
+    fix_dense_chunks(g);
     return t;
 }
 
