@@ -70,6 +70,7 @@ SIGNATURES = {
     "eg_copy_csc": ([_vp, _vp, _vp, _vp, _vp, _vp, _i32], _i32),
     "eg_cpbt_partition": ([_vp, _u32, _i32, _i32, _u64, _i32, _i32, _i32, _vp, _vp], _i32),
     "eg_optimal_offset": ([_vp, _u32, _u32, _vp], _i32),
+    "eg_cpbt_partition_noalloc": ([_vp, _u32, _i32, _i32, _u64, _i32, _i32, _vp, _vp, _vp], _i32),
     "eg_pagerank": ([_vp, _i32, _f32, _vp, _i32], _i32),
     "eg_bfs": ([_vp, _u32, _vp, _vp, _i32, _vp], _i32),
     "eg_cc": ([_vp, _vp, _i32], _i32),

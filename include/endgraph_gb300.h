@@ -133,6 +133,21 @@ int eg_cpbt_partition(const uint32_t* deg, uint32_t V, int P, int S, uint64_t et
 /* optimal_offset(a, n, k) core/graph.hpp:597-626 on the GPU; a on the host, offset[k+1] on host. */
 int eg_optimal_offset(const uint64_t* a, uint32_t n, uint32_t k, uint32_t* offset);
 
+/* eg_cpbt_partition for callers that cannot allocate device memory.  No counterpart in the
+ * reference.  Same boundaries as eg_cpbt_partition, but deg, partition_offset[P+1] and
+ * local_offset[P*(S+1)] (may be NULL) are all DEVICE pointers and the work is only enqueued on
+ * `stream` (a cudaStream_t; NULL is the legacy default stream).  It calls no cudaMalloc / cudaFree:
+ * its scratch is a fixed array inside the library, EG_NOALLOC_SCRATCH_BYTES per GPU, kept until
+ * process exit, which caps V, P and S at the limits below (larger requests return EG_ERR_INVALID).
+ * The first call on a device looks up that array's device address; make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race and must be serialised. */
+#define EG_NOALLOC_MAX_V (1u << 28)
+#define EG_NOALLOC_MAX_PARTITIONS 64
+#define EG_NOALLOC_MAX_SUB_PARTITIONS 16
+#define EG_NOALLOC_SCRATCH_BYTES (((1u << 28) / 4096u) * 16u + 16u * 1024u)
+int eg_cpbt_partition_noalloc(const uint32_t* deg, uint32_t V, int P, int S, uint64_t eta, int max_iterations,
+                              int dense, uint32_t* partition_offset, uint32_t* local_offset, void* stream);
+
 /* ---- toolkits: process_edges / process_vertices core/graph.hpp:1376-1817 ------------------ */
 /* Gemini PageRank (toolkits/pagerank.cpp:26-98): dense pull every iteration, FP32 ranks.
  * out[V] receives the final curr array. */
