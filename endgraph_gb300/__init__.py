@@ -55,6 +55,7 @@ SIGNATURES = {
     "eg_destroy": ([_vp], _i32),
     "eg_last_error": ([], ctypes.c_char_p),
     "eg_version": ([], _i32),
+    "eg_launch_count": ([], ctypes.c_ulonglong),
     "eg_stream": ([_vp], _vp),
     "eg_sync": ([_vp], _i32),
     "eg_load_edges": ([_vp, _vp, _u64, _u32, _i32, _i32, _i32], _i32),

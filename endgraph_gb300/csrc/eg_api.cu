@@ -78,6 +78,8 @@ extern "C" {
 
 int eg_version(void) { return 1; }
 
+unsigned long long eg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
 const char* eg_last_error(void) { return error_text(); }
 
 int eg_create(eg_graph** out, const eg_config* cfg) {

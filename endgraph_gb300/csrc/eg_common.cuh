@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <map>
 #include <string>
 #include <vector>
@@ -28,11 +29,15 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
         if (e_ != cudaSuccess) return ::eg::cuda_fail(e_, #call, __FILE__, __LINE__); \
     } while (0)
 
+// every kernel launch of the library is followed by this check, which also counts it
 #define EG_CHECK_LAUNCH(name)                                                  \
     do {                                                                       \
+        ::eg::g_launches.fetch_add(1, std::memory_order_relaxed);              \
         cudaError_t e_ = cudaGetLastError();                                   \
         if (e_ != cudaSuccess) return ::eg::cuda_fail(e_, name, __FILE__, __LINE__); \
     } while (0)
+
+extern std::atomic<unsigned long long> g_launches;
 
 #define EG_TRY(expr)                                                           \
     do {                                                                       \

@@ -682,7 +682,9 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
     {
         Timed t(&g->prof, g->stream, "bfs_init");
         k_fill_u32<<<gv, 256, 0, g->stream>>>(d_level, V, 0xFFFFFFFFu);
+        EG_CHECK_LAUNCH("k_fill_u32");
         k_fill_u32<<<gv, 256, 0, g->stream>>>(d_parent, V, V);
+        EG_CHECK_LAUNCH("k_fill_u32");
         EG_CUDA(cudaMemsetAsync(s.bm_visit.ptr, 0, bm_bytes, g->stream));
         EG_CUDA(cudaMemsetAsync(front, 0, bm_bytes, g->stream));
         EG_CUDA(cudaMemsetAsync(next_front, 0, bm_bytes, g->stream));
@@ -760,6 +762,7 @@ int run_sssp(eg_graph* g, uint32_t root, float* dist, int where) {
     {
         Timed t(&g->prof, g->stream, "sssp_init");
         k_fill_f32<<<grid_for(V, 256, 152u * 16u), 256, 0, g->stream>>>(d_dist, V, 1e9f);
+        EG_CHECK_LAUNCH("k_fill_f32");
         EG_CUDA(cudaMemsetAsync(s.bm_next.ptr, 0, bm_bytes, g->stream));
         k_sssp_root<<<1, 1, 0, g->stream>>>(d_dist, root, s.q0.as<uint32_t>());
         EG_CHECK_LAUNCH("k_sssp_root");
@@ -802,6 +805,7 @@ int run_cc(eg_graph* g, uint32_t* label, int where) {
     {
         Timed t(&g->prof, g->stream, "cc_init");
         k_iota<<<gv, 256, 0, g->stream>>>(d_label, V);  // cc.cpp:31-37
+        EG_CHECK_LAUNCH("k_iota");
         k_iota<<<gv, 256, 0, g->stream>>>(qa, V);       // active_in->fill()
         EG_CHECK_LAUNCH("k_iota");
         EG_CUDA(cudaMemsetAsync(s.bm_next.ptr, 0, bm_bytes, g->stream));

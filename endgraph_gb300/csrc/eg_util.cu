@@ -10,6 +10,7 @@
 namespace eg {
 
 static thread_local char t_err[512] = "";
+std::atomic<unsigned long long> g_launches{0};
 
 void set_error(const char* fmt, ...) {
     va_list ap;

@@ -93,6 +93,8 @@ int eg_create(eg_graph** out, const eg_config* cfg);
 int eg_destroy(eg_graph* g);
 const char* eg_last_error(void);
 int eg_version(void);
+/* kernels this process has launched through the library (all handles); no reference counterpart */
+unsigned long long eg_launch_count(void);
 void* eg_stream(eg_graph* g); /* the cudaStream_t all work of g is ordered on */
 int eg_sync(eg_graph* g);
 
