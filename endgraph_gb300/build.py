@@ -70,5 +70,31 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+TOOLKIT_SRC = os.path.join(HERE, "toolkits", "toolkits.cpp")
+TOOLKIT_DIR = os.path.join(HERE, "toolkits", "bin")
+TOOLKITS = ("pagerank", "bfs", "cc", "sssp")
+
+
+def build_toolkits() -> str:
+    """The C++ toolkit programs (host side over the C ABI via include/core/graph.hpp)."""
+    lib = build()
+    os.makedirs(TOOLKIT_DIR, exist_ok=True)
+    exe = os.path.join(TOOLKIT_DIR, "eg_toolkit")
+    deps = [TOOLKIT_SRC, lib] + glob.glob(os.path.join(INCLUDE, "core", "*.hpp"))
+    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(p) for p in deps):
+        cmd = ["g++", "-std=c++14", "-O2", "-Wall", f"-I{INCLUDE}", TOOLKIT_SRC, "-o", exe + ".tmp", f"-L{HERE}",
+               "-lendgraph_gb300", f"-Wl,-rpath,{HERE}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"toolkit build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(exe + ".tmp", exe)
+    for t in TOOLKITS:
+        link = os.path.join(TOOLKIT_DIR, t)
+        if not os.path.lexists(link):
+            os.symlink("eg_toolkit", link)
+    return TOOLKIT_DIR
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
+    print(build_toolkits())

@@ -1,0 +1,217 @@
+// graph.hpp — the Graph<EdgeData> API of EndGraph/Gemini (core/graph.hpp:100-1819 of the
+// reference) on one GB300 GPU, implemented over the C ABI of libendgraph_gb300 (endgraph_gb300.h).
+//
+// The reference's toolkits (toolkits/{pagerank,bfs,cc,sssp}.cpp) compile unchanged against this
+// header: it keeps the names, signatures, public fields and types they use.  What runs:
+//   - load_directed / load_undirected_from_directed read the binary edge file and build CPBT
+//     partition + CSR + CSC on the GPU; prep_time times the build only (like :1367-1371);
+//   - vertex arrays, subsets, gather/dump/restore are host-side helpers as in the reference;
+//   - the toolkits themselves run on the GPU through pagerank() / bfs() / cc() / sssp();
+//   - process_vertices / process_edges / emit with host std::function callbacks are accepted by the
+//     compiler but refused at run time (std::runtime_error, status EG_ERR_HOST_CALLBACK): host
+//     closures cannot execute on the device engine, and this library has no CPU engine to run them.
+// One GPU is one rank: partitions_num = 1, partition_idx = 0.
+#ifndef EG_CORE_GRAPH_HPP
+#define EG_CORE_GRAPH_HPP
+
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <unistd.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "core/atomic.hpp"
+#include "core/bitmap.hpp"
+#include "core/constants.hpp"
+#include "core/filesystem.hpp"
+#include "core/mpi.hpp"
+#include "core/time.hpp"
+#include "core/type.hpp"
+#include "endgraph_gb300.h"
+
+class EndGraphError : public std::runtime_error {
+   public:
+    int status;
+    EndGraphError(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+inline void eg_throw_if(int status, const char* what) {
+    if (status != EG_OK) throw EndGraphError(status, std::string(what) + ": " + eg_last_error());
+}
+
+template <typename EdgeData = Empty>
+class Graph {
+    static_assert(std::is_same<EdgeData, Empty>::value || sizeof(EdgeData) == 4,
+                  "the GPU structures hold no edge data or one 4-byte value per edge");
+
+   public:
+    // flags the toolkits set (core/graph.hpp:102-106; use_iteration / use_root are what the
+    // toolkits assign and the mode switch reads)
+    bool has_iterations = false, has_root = false;
+    bool use_undirected = false, use_iteration = false, use_root = false;
+    int max_iterations = 0;
+    size_t eta;
+    // one rank, one socket
+    int partitions_num = 1, partition_idx = 0, threads_num = 1, sockets_num = 1, threads_per_socket = 1;
+    UINT vertices_num = 0;
+    ULLONG read_edges_num = 0, edges_num = 0;
+    ULLONG exe_data = 0, prep_data = 0;
+    double prep_time = 0, exec_time = 0;
+    bool sparse = false;
+    UINT owned_vertices = 0;
+    UINT* degree = nullptr;                  // out-degree per vertex (host copy after load)
+    UINT partition_offset_storage[2] = {0, 0};
+    UINT local_partition_offset_storage[2] = {0, 0};
+    UINT* partition_offset = partition_offset_storage;
+    UINT* local_partition_offset = local_partition_offset_storage;
+
+    explicit Graph(int eta_) : eta((size_t)eta_) {
+        eg_config cfg;
+        cfg.eta = (uint64_t)eta_;
+        cfg.partitions = 1;
+        cfg.sub_partitions = 1;
+        cfg.max_iterations = 0;
+        cfg.device = 0;
+        cfg.stream = nullptr;
+        eg_throw_if(eg_create(&handle_, &cfg), "eg_create");
+    }
+    ~Graph() {
+        delete[] degree;
+        eg_destroy(handle_);
+    }
+    Graph(const Graph&) = delete;
+    Graph& operator=(const Graph&) = delete;
+
+    eg_graph* native() { return handle_; }
+
+    // ---- loading (core/graph.hpp:629-646, :1011-1084, :1358-1373) --------------------------
+    void load_directed(std::string path, UINT vertices) { load(path, vertices, false); }
+    void load_undirected_from_directed(std::string path, UINT vertices) { load(path, vertices, true); }
+
+    // ---- vertex arrays and subsets (core/graph.hpp:288-402) ----------------------------------
+    template <typename T>
+    T* alloc_vertex_array() {
+        void* p = mmap(nullptr, sizeof(T) * (size_t)vertices_num, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS,
+                       -1, 0);
+        if (p == MAP_FAILED) throw EndGraphError(EG_ERR_NOMEM, "alloc_vertex_array");
+        return (T*)p;
+    }
+    template <typename T>
+    void dealloc_vertex_array(T* array) {
+        munmap(array, sizeof(T) * (size_t)vertices_num);
+    }
+    template <typename T>
+    void fill_vertex_array(T* array, T value) {
+        for (UINT v = 0; v < vertices_num; ++v) array[v] = value;
+    }
+    VertexSubset* alloc_vertex_subset() { return new VertexSubset(vertices_num); }
+    template <typename T>
+    void gather_vertex_array(T*, int) {}  // one rank holds every vertex already
+    // raw sizeof(T) * V file, the reference's persistence format (core/graph.hpp:325-378)
+    template <typename T>
+    void dump_vertex_array(T* array, std::string path) {
+        FILE* f = fopen(path.c_str(), "wb");
+        if (!f) throw EndGraphError(EG_ERR_INVALID, "dump_vertex_array: cannot open " + path);
+        size_t n = fwrite(array, sizeof(T), vertices_num, f);
+        fclose(f);
+        if (n != vertices_num) throw EndGraphError(EG_ERR_INVALID, "dump_vertex_array: short write " + path);
+    }
+    template <typename T>
+    void restore_vertex_array(T* array, std::string path) {
+        if (file_size(path) != (long)(sizeof(T) * (size_t)vertices_num))
+            throw EndGraphError(EG_ERR_INVALID, "restore_vertex_array: size mismatch " + path);
+        FILE* f = fopen(path.c_str(), "rb");
+        size_t n = f ? fread(array, sizeof(T), vertices_num, f) : 0;
+        if (f) fclose(f);
+        if (n != vertices_num) throw EndGraphError(EG_ERR_INVALID, "restore_vertex_array: short read " + path);
+    }
+
+    // ---- host-callback engine entry points: compile-compatible, refused at run time ----------
+    template <typename R>
+    R process_vertices(std::function<R(UINT)>, VertexSubset*) {
+        refuse("process_vertices");
+        return R();
+    }
+    template <typename R, typename M>
+    R process_edges(std::function<void(UINT)>, std::function<R(UINT, M, AdjacentListType<EdgeData>)>,
+                    std::function<void(UINT, AdjacentListType<EdgeData>)>, std::function<R(UINT, M)>, VertexSubset*,
+                    VertexSubset* = nullptr) {
+        refuse("process_edges");
+        return R();
+    }
+    template <typename M>
+    void emit(UINT, M) {
+        refuse("emit");
+    }
+
+    // ---- the toolkits on the GPU (host output arrays of vertices_num entries) ------------------
+    // toolkits/pagerank.cpp:26-98 (FP32 ranks); returns the final curr array
+    void pagerank(int iterations, float* out, float damping = 0.85f) {
+        eg_throw_if(eg_pagerank(handle_, iterations, damping, out, EG_HOST), "eg_pagerank");
+    }
+    // toolkits/bfs.cpp:22-84; level and/or parent may be null
+    ULLONG bfs(UINT root, UINT* level, UINT* parent) {
+        uint64_t reached = 0;
+        eg_throw_if(eg_bfs(handle_, root, level, parent, EG_HOST, &reached), "eg_bfs");
+        return reached;
+    }
+    // toolkits/cc.cpp:22-84 (load_undirected_from_directed first)
+    void cc(UINT* label) { eg_throw_if(eg_cc(handle_, label, EG_HOST), "eg_cc"); }
+    // toolkits/sssp.cpp:24-84 (Graph<float>)
+    void sssp(UINT root, float* dist) { eg_throw_if(eg_sssp(handle_, root, dist, EG_HOST), "eg_sssp"); }
+
+   private:
+    eg_graph* handle_ = nullptr;
+
+    [[noreturn]] void refuse(const char* what) {
+        throw EndGraphError(EG_ERR_HOST_CALLBACK,
+                            std::string(what) +
+                                ": host std::function callbacks cannot run on the GB300 engine; use "
+                                "Graph::pagerank/bfs/cc/sssp or the eg_* C ABI");
+    }
+
+    void load(const std::string& path, UINT vertices, bool symmetric) {
+        long bytes = file_size(path);
+        if (bytes < 0) throw EndGraphError(EG_ERR_INVALID, "cannot stat " + path);
+        const size_t rec = sizeof(EdgeType<EdgeData>);
+        const ULLONG n = (ULLONG)bytes / rec;
+        std::vector<char> buf(n * rec + 1);
+        int fd = open(path.c_str(), O_RDONLY);
+        if (fd < 0) throw EndGraphError(EG_ERR_INVALID, "cannot open " + path);
+        size_t done = 0;
+        while (done < n * rec) {  // CHUNKSIZE records per read, like preload_graph_file
+            size_t want = n * rec - done;
+            if (want > (size_t)CHUNKSIZE * rec) want = (size_t)CHUNKSIZE * rec;
+            ssize_t got = read(fd, buf.data() + done, want);
+            if (got <= 0) break;
+            done += (size_t)got;
+        }
+        close(fd);
+        if (done != n * rec) throw EndGraphError(EG_ERR_INVALID, "short read " + path);
+        vertices_num = vertices;
+        edges_num = symmetric ? 2 * n : n;
+        read_edges_num = edges_num;
+        owned_vertices = vertices;
+        eg_throw_if(eg_load_edges(handle_, buf.data(), n, vertices, (int)rec, symmetric ? 1 : 0, EG_HOST),
+                    "eg_load_edges");
+        double t = -MPI_Wtime();
+        eg_throw_if(eg_build(handle_, 1, 1), "eg_build");
+        t += MPI_Wtime();
+        prep_time = t;
+        delete[] degree;
+        degree = new UINT[vertices];
+        eg_throw_if(eg_get_degrees(handle_, degree, nullptr, EG_HOST), "eg_get_degrees");
+        eg_throw_if(eg_get_partition(handle_, partition_offset_storage, local_partition_offset_storage),
+                    "eg_get_partition");
+    }
+};
+
+#endif
