@@ -78,6 +78,11 @@ SIGNATURES = {
     "eg_sssp": ([_vp, _u32, _vp, _i32], _i32),
     "eg_last_run": ([_vp, _vp, _vp, _vp, _vp], _i32),
     "eg_set_option": ([_vp, _i32, ctypes.c_int64], _i32),
+    "eg_msbfs": ([_vp, _vp, _i32, _vp, _i32, _vp], _i32),
+    "eg_sssp_batch": ([_vp, _vp, _i32, _vp, _i32], _i32),
+    "eg_load_directed_with_ids": ([_vp, _vp, _u64, _u32, _i32], _i32),
+    "eg_ppr": ([_vp, _vp, _vp, _i32, _f32, _i32, _vp, _i32], _i32),
+    "eg_ppr_backward": ([_vp, _vp, _vp, _i32, _f32, _i32, _vp, _vp, _i32], _i32),
     "eg_generate_rmat": ([_vp, _i32, _u64, _u32, _f64, _f64, _f64, _u64, _i32, _f32, _f32, _vp], _i32),
     "eg_profile_enable": ([_vp, _i32], _i32),
     "eg_profile_reset": ([_vp], _i32),
@@ -127,6 +132,11 @@ def _buf(x):
     if not x.flags["C_CONTIGUOUS"]:
         raise ValueError("array must be C-contiguous")
     return ctypes.c_void_p(x.ctypes.data), EG_HOST
+
+
+def _to_device_u32(a, like):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).to(like.device)
 
 
 def pack_edges(src, dst, w=None):
@@ -285,6 +295,65 @@ class Graph:
         p, where = _buf(dist)
         _check(self._L.eg_sssp(self.h, root, p, where))
         return dist
+
+    def load_directed_with_ids(self, edges, V):
+        edges, E, rec = self._records(edges)
+        if rec != 8:
+            raise ValueError("eg_load_directed_with_ids takes {src, dst} records")
+        p, where = _buf(edges)
+        _check(self._L.eg_load_directed_with_ids(self.h, p, E, V, where))
+
+    def msbfs(self, roots, levels=None):
+        roots = np.ascontiguousarray(roots, np.uint32)
+        V = self.info().V
+        if levels is None:
+            levels = np.empty((len(roots), V), np.uint8)
+        p, where = _buf(levels)
+        if where == EG_DEVICE:
+            import torch
+            roots_t = torch.from_numpy(roots.view(np.int32)).to(levels.device)
+            rp = _buf(roots_t)[0]
+        else:
+            rp = _buf(roots)[0]
+        e = ctypes.c_uint64()
+        _check(self._L.eg_msbfs(self.h, rp, len(roots), p, where, ctypes.byref(e)))
+        return levels, e.value
+
+    def sssp_batch(self, sources, dist=None):
+        sources = np.ascontiguousarray(sources, np.uint32)
+        V = self.info().V
+        if dist is None:
+            dist = np.empty((len(sources), V), np.float32)
+        p, where = _buf(dist)
+        if where == EG_DEVICE:
+            import torch
+            sp = _buf(torch.from_numpy(sources.view(np.int32)).to(dist.device))[0]
+        else:
+            sp = _buf(sources)[0]
+        _check(self._L.eg_sssp_batch(self.h, sp, len(sources), p, where))
+        return dist
+
+    def ppr(self, weights, seeds, alpha=0.15, iterations=50, out=None):
+        """weights and out on the host (numpy) or all on the device (torch)."""
+        seeds = np.ascontiguousarray(seeds, np.uint32)
+        V = self.info().V
+        if out is None:
+            out = np.empty((len(seeds), V), np.float32)
+        wp, where = _buf(weights)
+        op, _ = _buf(out)
+        sp = _buf(seeds)[0] if where == EG_HOST else _buf(_to_device_u32(seeds, weights))[0]
+        _check(self._L.eg_ppr(self.h, wp, sp, len(seeds), alpha, iterations, op, where))
+        return out
+
+    def ppr_backward(self, weights, seeds, dl_dx, alpha=0.15, iterations=50, dl_dw=None):
+        seeds = np.ascontiguousarray(seeds, np.uint32)
+        if dl_dw is None:
+            dl_dw = np.empty(len(weights), np.float32)
+        wp, where = _buf(weights)
+        sp = _buf(seeds)[0] if where == EG_HOST else _buf(_to_device_u32(seeds, weights))[0]
+        _check(self._L.eg_ppr_backward(self.h, wp, sp, len(seeds), alpha, iterations, _buf(dl_dx)[0], _buf(dl_dw)[0],
+                                       where))
+        return dl_dw
 
     def set_option(self, option, value):
         _check(self._L.eg_set_option(self.h, option, value))

@@ -61,6 +61,7 @@ void free_handle(eg_graph* g) {
     cudaSetDevice(g->device);
     if (g->stream) cudaStreamSynchronize(g->stream);
     g->prof.clear();
+    free_batch_state(g);
     if (g->pinned) cudaFreeHost(g->pinned);
     cudaStream_t s = g->stream;
     bool own = g->own_stream;
@@ -137,8 +138,11 @@ int eg_load_edges(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int ed
     }
     g->built_csr = g->built_csc = false;
     g->eng.pull_ready = false;
+    free_batch_state(g);
     g->V = V;
     g->E = total;
+    g->E_input = E;
+    g->edge_ids = false;
     g->edge_bytes = edge_bytes;
     g->weighted = edge_bytes == 12;
     g->symmetric = symmetric != 0;
@@ -158,7 +162,57 @@ int eg_build(eg_graph* g, int want_csr, int want_csc) {
         set_error("eg_build: no edge list loaded");
         return EG_ERR_STATE;
     }
+    free_batch_state(g);
     return build_structures(g, want_csr, want_csc);
+}
+
+int eg_load_directed_with_ids(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int where) {
+    EG_TRY(check_graph(g, "eg_load_directed_with_ids"));
+    if (V == 0 || (E > 0 && !edges) || E >= (1ull << 32) || (where != EG_HOST && where != EG_DEVICE)) {
+        set_error("eg_load_directed_with_ids: need V > 0, an edge pointer, E < 2^32 and a valid `where`");
+        return EG_ERR_INVALID;
+    }
+    g->built_csr = g->built_csc = false;
+    g->eng.pull_ready = false;
+    free_batch_state(g);
+    g->V = V;
+    g->E = E;
+    g->E_input = E;
+    g->edge_bytes = 12;
+    g->weighted = 1;
+    g->symmetric = 0;
+    g->edge_ids = true;
+    EG_TRY(g->edges.reserve((size_t)E * 12 + 64));
+    EG_TRY(g->bucketed.reserve((size_t)E * 8 + 64));
+    if (E) {
+        EG_CUDA(cudaMemcpyAsync(g->bucketed.ptr, edges, (size_t)E * 8,
+                                where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, g->stream));
+        EG_TRY(expand_with_ids(g, g->bucketed.as<uint8_t>(), E));
+    }
+    EG_TRY(validate_edges(g, E));
+    return build_structures(g, 1, 1);
+}
+
+int eg_msbfs(eg_graph* g, const uint32_t* roots, int nroots, uint8_t* levels, int where, uint64_t* edges) {
+    EG_TRY(check_graph(g, "eg_msbfs"));
+    return run_msbfs(g, roots, nroots, levels, where, edges);
+}
+
+int eg_ppr(eg_graph* g, const float* weights, const uint32_t* seeds, int nseeds, float alpha, int iterations,
+           float* out, int where) {
+    EG_TRY(check_graph(g, "eg_ppr"));
+    return run_ppr(g, weights, seeds, nseeds, alpha, iterations, out, where);
+}
+
+int eg_ppr_backward(eg_graph* g, const float* weights, const uint32_t* seeds, int nseeds, float alpha, int iterations,
+                    const float* dl_dx, float* dl_dw, int where) {
+    EG_TRY(check_graph(g, "eg_ppr_backward"));
+    return run_ppr_backward(g, weights, seeds, nseeds, alpha, iterations, dl_dx, dl_dw, where);
+}
+
+int eg_sssp_batch(eg_graph* g, const uint32_t* sources, int nsources, float* dist, int where) {
+    EG_TRY(check_graph(g, "eg_sssp_batch"));
+    return run_sssp_batch(g, sources, nsources, dist, where);
 }
 
 int eg_load_directed(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int where) {

@@ -1,0 +1,818 @@
+// eg_batch.cu — batched operators over one built graph (no reference counterpart; they batch the
+// toolkits of toolkits/{bfs,sssp}.cpp and a personalised PageRank built on pagerank.cpp):
+//
+//  * eg_msbfs: bit-parallel BFS from up to 64 roots.  Every vertex keeps a u64 of the roots that
+//    reached it and a u64 of the roots whose frontier it is in; a level is one chunked pull over
+//    the CSC that ORs the in-neighbours' frontier words (exact integer work, levels identical to
+//    64 separate BFS runs).
+//  * 64-column row engine: a destination's 64 values (one per seed / source) sit in one 256-byte
+//    row; one warp reduces a task of <= kTaskEdges in-edges, each lane owning two columns, so every
+//    gathered row is a single coalesced 256-byte read.  Lists longer than a task are split and
+//    their partial rows combined in a small per-heavy-vertex buffer.  Used by
+//      - eg_ppr: personalised PageRank x_{k+1} = a*e_seed + (1-a) * A^T x_k, A = row-normalised
+//        edge weights, FP32;
+//      - eg_ppr_backward: the adjoint of K unrolled iterations.  lambda_k = (1-a) A lambda_{k+1} is
+//        a pull over the CSR (the transpose of the forward CSC); the same sweep accumulates
+//        dL/dA_uv = (1-a) sum_k <x_k[u], lambda_{k+1}[v]>; iterates x_k are recomputed from
+//        checkpoints kept every ceil(sqrt(K)) steps;
+//      - eg_sssp_batch: Bellman-Ford from up to 64 sources, in place, skipping sources whose
+//        distance did not change in the previous sweep (bit-exact least fixpoint).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "eg_pull.cuh"
+
+namespace eg {
+
+constexpr uint32_t kTaskEdges = 512;
+constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
+constexpr int kRowWarps = 8;  // 256-thread blocks
+
+// ---------------------------------------------------------------------------------------------
+// MS-BFS
+struct MsBfsPullOp {
+    using Acc = unsigned long long;
+    static constexpr bool kFilter = true;
+    const unsigned long long* front;
+    unsigned long long* visit;
+    unsigned long long* next;
+    uint8_t* levels;  // [V][64], 0xFF = unreached
+    uint32_t next_level;
+    unsigned long long full;
+    uint32_t* n_new;
+    unsigned long long* reach_edges;
+    const uint32_t* deg;
+    __device__ bool item_active(uint32_t v) const { return __ldcg(visit + v) != full; }
+    __device__ Acc identity() const { return 0ull; }
+    __device__ Acc gather(uint32_t u, uint64_t) const { return __ldcg(front + u); }
+    __device__ Acc combine(Acc a, Acc b) const { return a | b; }
+    __device__ void smem_add(Acc* slot, Acc v) const {
+        if (v) atomicOr(slot, v);
+    }
+    __device__ void finish(bool ok, uint32_t v, Acc m, bool) const {
+        unsigned long long nb = 0;
+        if (ok && m) {
+            const unsigned long long old = atomicOr(visit + v, m);
+            nb = m & ~old;
+            if (nb) {
+                atomicOr(next + v, nb);
+                atomicAdd(reach_edges, (unsigned long long)__popcll(nb) * deg[v]);
+                if (levels) {
+                    unsigned long long b = nb;
+                    while (b) {
+                        const int s = __ffsll((long long)b) - 1;
+                        b &= b - 1;
+                        levels[(uint64_t)v * 64 + s] = (uint8_t)next_level;
+                    }
+                }
+            }
+        }
+        const unsigned any = __ballot_sync(0xffffffffu, nb != 0);
+        if ((threadIdx.x & 31) == 0 && any) atomicAdd(n_new, (uint32_t)__popc(any));
+    }
+};
+
+__global__ void k_msbfs_roots(const uint32_t* roots, int n, unsigned long long* visit, unsigned long long* front,
+                              uint8_t* levels, unsigned long long* reach_edges, const uint32_t* deg) {
+    int s = threadIdx.x;
+    if (s < n) {
+        const uint32_t r = roots[s];
+        atomicOr(visit + r, 1ull << s);
+        atomicOr(front + r, 1ull << s);
+        if (levels) levels[(uint64_t)r * 64 + s] = 0;
+        atomicAdd(reach_edges, (unsigned long long)deg[r]);
+    }
+}
+
+// [V][64] -> [n][V] for the first n columns (32x32 tiles through shared memory)
+__global__ void k_transpose_u8(const uint8_t* __restrict__ in, uint32_t V, int n, uint8_t* __restrict__ out) {
+    __shared__ uint8_t t[64][33];
+    const uint64_t v0 = (uint64_t)blockIdx.x * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const uint64_t v = v0 + i;
+        for (int s = threadIdx.x; s < 64; s += blockDim.x) t[s][i] = v < V ? in[v * 64 + s] : 0;
+    }
+    __syncthreads();
+    for (int s = threadIdx.y; s < n; s += blockDim.y) {
+        const uint64_t v = v0 + threadIdx.x;
+        if (v < V) out[(uint64_t)s * V + v] = t[s][threadIdx.x];
+    }
+}
+
+template <typename T>
+__global__ void k_transpose_rows(const T* __restrict__ in, uint32_t V, int n, T* __restrict__ out) {
+    __shared__ T t[64][33];
+    const uint64_t v0 = (uint64_t)blockIdx.x * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const uint64_t v = v0 + i;
+        for (int s = threadIdx.x; s < 64; s += blockDim.x) t[s][i] = v < V ? in[v * 64 + s] : T(0);
+    }
+    __syncthreads();
+    for (int s = threadIdx.y; s < n; s += blockDim.y) {
+        const uint64_t v = v0 + threadIdx.x;
+        if (v < V) out[(uint64_t)s * V + v] = t[s][threadIdx.x];
+    }
+}
+
+template <typename T>
+__global__ void k_untranspose_rows(const T* __restrict__ in, uint32_t V, int n, T* __restrict__ out) {
+    __shared__ T t[64][33];
+    const uint64_t v0 = (uint64_t)blockIdx.x * 32;
+    for (int s = threadIdx.y; s < 64; s += blockDim.y) {
+        const uint64_t v = v0 + threadIdx.x;
+        t[s][threadIdx.x] = (s < n && v < V) ? in[(uint64_t)s * V + v] : T(0);
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const uint64_t v = v0 + i;
+        for (int s = threadIdx.x; s < 64; s += blockDim.x)
+            if (v < V) out[v * 64 + s] = t[s][i];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// tasks: item i of a list index (begin[i], begin[i+1]) split into pieces of <= kTaskEdges edges
+struct TaskLoad {
+    const uint64_t* begin;
+    __device__ uint32_t operator()(uint64_t i) const {
+        const uint64_t n = begin[i + 1] - begin[i];
+        return (uint32_t)((n + kTaskEdges - 1) / kTaskEdges);
+    }
+};
+struct TaskEpi {
+    uint32_t* t_item;
+    uint32_t* t_part;
+    uint32_t* heavy_slot;     // per item
+    uint32_t* heavy_item;     // per slot
+    uint32_t* nheavy;
+    __device__ void operator()(uint64_t i, uint64_t excl, uint32_t cnt) const {
+        for (uint32_t p = 0; p < cnt; ++p) {
+            t_item[excl + p] = (uint32_t)i;
+            t_part[excl + p] = p;
+        }
+        uint32_t slot = kNoSlot;
+        if (cnt > 1) {
+            slot = atomicAdd(nheavy, 1u);
+            heavy_item[slot] = (uint32_t)i;
+        }
+        heavy_slot[i] = slot;
+    }
+};
+
+struct RowTasks {
+    DevBuf item, part, heavy_slot, heavy_item, counts;
+    uint64_t ntasks = 0;
+    uint32_t nheavy = 0;
+    uint64_t nitems = 0;
+    const uint64_t* begin = nullptr;
+};
+
+static int make_tasks(eg_graph* g, RowTasks& t, const uint64_t* begin, uint64_t nitems) {
+    // upper bound on tasks: items + E / kTaskEdges
+    const uint64_t cap = nitems + g->E / kTaskEdges + 2;
+    EG_TRY(t.item.reserve(sizeof(uint32_t) * cap));
+    EG_TRY(t.part.reserve(sizeof(uint32_t) * cap));
+    EG_TRY(t.heavy_slot.reserve(sizeof(uint32_t) * (nitems + 1)));
+    EG_TRY(t.heavy_item.reserve(sizeof(uint32_t) * (g->E / kTaskEdges + 2)));
+    EG_TRY(t.counts.reserve(32));
+    EG_CUDA(cudaMemsetAsync(t.counts.ptr, 0, 32, g->stream));
+    uint64_t* d_total = t.counts.as<uint64_t>();
+    uint32_t* d_nheavy = reinterpret_cast<uint32_t*>(t.counts.as<uint64_t>() + 1);
+    TaskEpi ep{t.item.as<uint32_t>(), t.part.as<uint32_t>(), t.heavy_slot.as<uint32_t>(), t.heavy_item.as<uint32_t>(),
+               d_nheavy};
+    EG_TRY(launch_scan(g, TaskLoad{begin}, ep, nitems, d_total, "row_tasks"));
+    uint64_t h[2] = {0, 0};
+    EG_CUDA(cudaMemcpyAsync(h, t.counts.ptr, 16, cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    t.ntasks = nitems ? h[0] : 0;
+    t.nheavy = (uint32_t)(h[1] & 0xFFFFFFFFu);
+    t.nitems = nitems;
+    t.begin = begin;
+    return EG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// row kernels: warp per task, lane l owns columns 2l, 2l+1 of a 64-column row (float2)
+struct RowArgs {
+    const uint32_t* t_item;
+    const uint32_t* t_part;
+    uint64_t ntasks;
+    const uint32_t* heavy_slot;
+    const uint32_t* item_vertex;  // null: item index is the vertex
+    const uint64_t* begin;        // list offsets per item (item i: [begin[i], begin[i+1]))
+    const uint32_t* adj;
+    const float* w;               // per-edge weight (normalised for PPR, raw for SSSP)
+};
+
+// PPR forward: y[v] = (1-a) * sum_{u in in(v)} wn_uv * x[u]
+__global__ void __launch_bounds__(256) k_row_spmm(RowArgs a, const float2* __restrict__ x, float2* __restrict__ y,
+                                                   float2* __restrict__ heavy_acc, float scale) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t t = warp; t < a.ntasks; t += nwarps) {
+        const uint32_t it = a.t_item[t];
+        const uint64_t lb = a.begin[it], le = a.begin[it + 1];
+        const uint64_t e0 = lb + (uint64_t)a.t_part[t] * kTaskEdges;
+        const uint64_t e1 = e0 + kTaskEdges < le ? e0 + kTaskEdges : le;
+        float2 acc = make_float2(0.f, 0.f);
+        uint64_t e = e0;
+        for (; e + 4 <= e1; e += 4) {
+            uint32_t u[4];
+            float wv[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                u[j] = __ldg(a.adj + e + j);
+                wv[j] = __ldg(a.w + e + j);
+            }
+            float2 r[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) r[j] = __ldcg(x + (uint64_t)u[j] * 32 + lane);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                acc.x = fmaf(wv[j], r[j].x, acc.x);
+                acc.y = fmaf(wv[j], r[j].y, acc.y);
+            }
+        }
+        for (; e < e1; ++e) {
+            const uint32_t u = __ldg(a.adj + e);
+            const float wv = __ldg(a.w + e);
+            const float2 r = __ldcg(x + (uint64_t)u * 32 + lane);
+            acc.x = fmaf(wv, r.x, acc.x);
+            acc.y = fmaf(wv, r.y, acc.y);
+        }
+        const uint32_t v = a.item_vertex ? a.item_vertex[it] : it;
+        const uint32_t slot = a.heavy_slot[it];
+        if (slot == kNoSlot) {
+            y[(uint64_t)v * 32 + lane] = make_float2(scale * acc.x, scale * acc.y);
+        } else {
+            atomicAdd(&heavy_acc[(uint64_t)slot * 32 + lane].x, acc.x);
+            atomicAdd(&heavy_acc[(uint64_t)slot * 32 + lane].y, acc.y);
+        }
+    }
+}
+
+__global__ void k_row_heavy_finish(const uint32_t* __restrict__ heavy_item, const uint32_t* __restrict__ item_vertex,
+                                   uint32_t nheavy, float2* __restrict__ heavy_acc, float2* __restrict__ y, float scale) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t slot = i >> 5;
+    const int lane = threadIdx.x & 31;
+    if (slot >= nheavy) return;
+    const uint32_t it = heavy_item[slot];
+    const uint32_t v = item_vertex ? item_vertex[it] : it;
+    const float2 a = heavy_acc[slot * 32 + lane];
+    heavy_acc[slot * 32 + lane] = make_float2(0.f, 0.f);
+    y[(uint64_t)v * 32 + lane] = make_float2(scale * a.x, scale * a.y);
+}
+
+// y[seed_s][s] += a
+__global__ void k_ppr_teleport(const uint32_t* seeds, int n, float* y, float alpha) {
+    const int s = threadIdx.x;
+    if (s < n) atomicAdd(y + (uint64_t)seeds[s] * 64 + s, alpha);
+}
+__global__ void k_ppr_init(const uint32_t* seeds, int n, float* x) {
+    const int s = threadIdx.x;
+    if (s < n) x[(uint64_t)seeds[s] * 64 + s] = 1.0f;
+}
+
+// normalised weights: wn[e] = w[eid[e]] / s[src], s[u] = sum of u's out-weights
+__global__ void k_out_weight_sums(const uint64_t* __restrict__ csr_off, const float* __restrict__ csr_eid,
+                                  const float* __restrict__ w_in, uint32_t V, float* __restrict__ s) {
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < V; u += (uint64_t)gridDim.x * blockDim.x) {
+        double acc = 0;
+        for (uint64_t e = csr_off[u]; e < csr_off[u + 1]; ++e) acc += w_in[__float_as_uint(csr_eid[e])];
+        s[u] = (float)acc;
+    }
+}
+__global__ void k_gather_norm_w(const uint32_t* __restrict__ nbr_is_src, const float* __restrict__ eid,
+                                const float* __restrict__ w_in, const float* __restrict__ s, uint64_t E,
+                                float* __restrict__ wn) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t id = __float_as_uint(eid[e]);
+        wn[e] = w_in[id] / s[nbr_is_src[e]];
+    }
+}
+// CSR positions: the source of position e is the row it sits in
+__global__ void k_row_of(const uint64_t* __restrict__ off, uint32_t V, uint32_t* __restrict__ row) {
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < V; u += (uint64_t)gridDim.x * blockDim.x)
+        for (uint64_t e = off[u]; e < off[u + 1]; ++e) row[e] = (uint32_t)u;
+}
+
+// ---- adjoint sweep over the CSR: for a source row u,
+//   lam_out[u] = (1-a) * sum_{v in out(u)} wn_uv * lam_in[v]
+//   gA[e]     += (1-a) * <x_k[u], lam_in[v]>      (per CSR edge e = (u, v))
+__global__ void __launch_bounds__(256) k_row_adjoint(RowArgs a, const float2* __restrict__ lam_in,
+                                                      const float2* __restrict__ xk, float2* __restrict__ lam_out,
+                                                      float2* __restrict__ heavy_acc, float* __restrict__ gA,
+                                                      float scale) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t t = warp; t < a.ntasks; t += nwarps) {
+        const uint32_t u = a.t_item[t];  // CSR items are vertices
+        const uint64_t lb = a.begin[u], le = a.begin[u + 1];
+        const uint64_t e0 = lb + (uint64_t)a.t_part[t] * kTaskEdges;
+        const uint64_t e1 = e0 + kTaskEdges < le ? e0 + kTaskEdges : le;
+        const float2 xu = __ldcg(xk + (uint64_t)u * 32 + lane);
+        float2 acc = make_float2(0.f, 0.f);
+        for (uint64_t e = e0; e < e1; ++e) {
+            const uint32_t v = __ldg(a.adj + e);
+            const float wv = __ldg(a.w + e);
+            const float2 l = __ldcg(lam_in + (uint64_t)v * 32 + lane);
+            acc.x = fmaf(wv, l.x, acc.x);
+            acc.y = fmaf(wv, l.y, acc.y);
+            float d = fmaf(xu.x, l.x, xu.y * l.y);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+            if (lane == 0) gA[e] = fmaf(scale, d, gA[e]);
+        }
+        const uint32_t slot = a.heavy_slot[u];
+        if (slot == kNoSlot) {
+            lam_out[(uint64_t)u * 32 + lane] = make_float2(scale * acc.x, scale * acc.y);
+        } else {
+            atomicAdd(&heavy_acc[(uint64_t)slot * 32 + lane].x, acc.x);
+            atomicAdd(&heavy_acc[(uint64_t)slot * 32 + lane].y, acc.y);
+        }
+    }
+}
+
+// dL/dw_e = (gA_e - sum_{e' in row(u)} wn_e' gA_e') / s_u, scattered to the input edge order
+__global__ void k_weight_grad(const uint64_t* __restrict__ off, uint32_t V, const float* __restrict__ wn,
+                              const float* __restrict__ gA, const float* __restrict__ s,
+                              const float* __restrict__ eid, float* __restrict__ dw) {
+    for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < V; u += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t b = off[u], e1 = off[u + 1];
+        if (b == e1) continue;
+        double dot = 0;
+        for (uint64_t e = b; e < e1; ++e) dot += (double)wn[e] * gA[e];
+        const float inv = 1.0f / s[u];
+        for (uint64_t e = b; e < e1; ++e) dw[__float_as_uint(eid[e])] = (float)(((double)gA[e] - dot) * inv);
+    }
+}
+
+// lam_K = dL/dx_K given in [V][64]; nothing else to seed
+// ---- batched SSSP: in place, skipping sources whose row did not change in the last sweep --------
+__global__ void __launch_bounds__(256) k_row_sssp(RowArgs a, float2* __restrict__ dist,
+                                                   const uint8_t* __restrict__ changed_prev,
+                                                   uint8_t* __restrict__ changed_next, int* __restrict__ any) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t t = warp; t < a.ntasks; t += nwarps) {
+        const uint32_t it = a.t_item[t];
+        const uint64_t lb = a.begin[it], le = a.begin[it + 1];
+        const uint64_t e0 = lb + (uint64_t)a.t_part[t] * kTaskEdges;
+        const uint64_t e1 = e0 + kTaskEdges < le ? e0 + kTaskEdges : le;
+        float2 best = make_float2(1e9f, 1e9f);
+        for (uint64_t e = e0; e < e1; ++e) {
+            const uint32_t u = __ldg(a.adj + e);
+            if (!__ldcg(changed_prev + u)) continue;  // uniform across the warp
+            const float wv = __ldg(a.w + e);
+            const float2 du = __ldcg(dist + (uint64_t)u * 32 + lane);
+            best.x = fminf(best.x, du.x + wv);  // toolkits/sssp.cpp:55: relax_dist = msg + w
+            best.y = fminf(best.y, du.y + wv);
+        }
+        const uint32_t v = a.item_vertex[it];
+        float2* dv = dist + (uint64_t)v * 32 + lane;
+        bool lowered = false;
+        if (best.x < __ldcg(&dv->x)) lowered |= best.x < __int_as_float(atomicMin(reinterpret_cast<int*>(&dv->x), __float_as_int(best.x)));
+        if (best.y < __ldcg(&dv->y)) lowered |= best.y < __int_as_float(atomicMin(reinterpret_cast<int*>(&dv->y), __float_as_int(best.y)));
+        if (__any_sync(0xffffffffu, lowered) && lane == 0) {
+            changed_next[v] = 1;
+            *any = 1;
+        }
+    }
+}
+
+__global__ void k_fill_f32_rows(float* p, uint64_t n, float v) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+__global__ void k_sssp_batch_init(const uint32_t* srcs, int n, float* dist, uint8_t* changed) {
+    const int s = threadIdx.x;
+    if (s < n) {
+        dist[(uint64_t)srcs[s] * 64 + s] = 0.f;
+        changed[srcs[s]] = 1;
+    }
+}
+
+// {src, dst} records -> {src, dst, index} records: the index rides through the build in the weight
+// slot, so every CSR / CSC position knows which input edge it holds
+__global__ void k_expand_ids(const uint2* __restrict__ in, uint64_t E, uint32_t* __restrict__ out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < E; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint2 r = in[i];
+        out[3 * i] = r.x;
+        out[3 * i + 1] = r.y;
+        out[3 * i + 2] = (uint32_t)i;
+    }
+}
+
+int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E) {
+    if (!E) return EG_OK;
+    k_expand_ids<<<grid_for(E, 256, 152u * 16u), 256, 0, g->stream>>>(reinterpret_cast<const uint2*>(rec8_dev), E,
+                                                                      g->edges.as<uint32_t>());
+    EG_CHECK_LAUNCH("k_expand_ids");
+    return EG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+struct BatchState {
+    DevBuf a64, b64, c64, lev, rows0, rows1, heavy, tmp_out, seeds, wn_csc, wn_csr, s_out, gA, row_of, ck, seg;
+    DevBuf ch0, ch1, flag;
+    RowTasks csc_tasks, csr_tasks;
+    bool csc_ready = false, csr_ready = false;
+};
+
+static BatchState& bstate(eg_graph* g) {
+    if (!g->batch) g->batch = new BatchState();
+    return *static_cast<BatchState*>(g->batch);
+}
+
+void free_batch_state(eg_graph* g) {
+    delete static_cast<BatchState*>(g->batch);
+    g->batch = nullptr;
+}
+
+static int copy_small_in(eg_graph* g, DevBuf& dst, const uint32_t* src, int n, int where) {
+    EG_TRY(dst.reserve(sizeof(uint32_t) * 64));
+    EG_CUDA(cudaMemcpyAsync(dst.ptr, src, sizeof(uint32_t) * n,
+                            where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, g->stream));
+    return EG_OK;
+}
+
+static int check_roots(eg_graph* g, const uint32_t* roots, int n, int where, const char* fn) {
+    if (!roots || n < 1 || n > 64) {
+        set_error("%s: need 1..64 roots", fn);
+        return EG_ERR_INVALID;
+    }
+    std::vector<uint32_t> h(n);
+    EG_CUDA(cudaMemcpy(h.data(), roots, sizeof(uint32_t) * n,
+                       where == EG_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+    for (int i = 0; i < n; ++i)
+        if (h[i] >= g->V) {
+            set_error("%s: root %u >= V %u", fn, h[i], g->V);
+            return EG_ERR_INVALID;
+        }
+    return EG_OK;
+}
+
+int run_msbfs(eg_graph* g, const uint32_t* roots, int n, uint8_t* levels, int where, uint64_t* edges) {
+    if (!g->built_csc) { set_error("eg_msbfs: CSC not built"); return EG_ERR_STATE; }
+    EG_TRY(check_roots(g, roots, n, where, "eg_msbfs"));
+    EG_TRY(ensure_engine(g));
+    EG_TRY(setup_pull(g));
+    BatchState& b = bstate(g);
+    const uint64_t V = g->V;
+    EG_TRY(b.a64.reserve(8 * V + 8));
+    EG_TRY(b.b64.reserve(8 * V + 8));
+    EG_TRY(b.c64.reserve(8 * V + 8));
+    if (levels) EG_TRY(b.lev.reserve(64 * V + 64));
+    EG_TRY(copy_small_in(g, b.seeds, roots, n, where));
+    unsigned long long* visit = b.a64.as<unsigned long long>();
+    unsigned long long* front = b.b64.as<unsigned long long>();
+    unsigned long long* next = b.c64.as<unsigned long long>();
+    uint8_t* lev = levels ? b.lev.as<uint8_t>() : nullptr;
+    uint32_t* d_new = reinterpret_cast<uint32_t*>(g->eng.counters.as<unsigned long long>() + 2);
+    unsigned long long* d_reach = g->eng.counters.as<unsigned long long>() + 4;
+    {
+        Timed t(&g->prof, g->stream, "msbfs_init");
+        EG_CUDA(cudaMemsetAsync(visit, 0, 8 * V, g->stream));
+        EG_CUDA(cudaMemsetAsync(front, 0, 8 * V, g->stream));
+        EG_CUDA(cudaMemsetAsync(d_reach, 0, 8, g->stream));
+        if (lev) EG_CUDA(cudaMemsetAsync(lev, 0xFF, 64 * V, g->stream));
+        k_msbfs_roots<<<1, 64, 0, g->stream>>>(b.seeds.as<uint32_t>(), n, visit, front, lev, d_reach, g->outdeg.as<uint32_t>());
+        EG_CHECK_LAUNCH("k_msbfs_roots");
+    }
+    const unsigned long long full = n == 64 ? ~0ull : ((1ull << n) - 1ull);
+    uint32_t lvl = 0;
+    int sweeps = 0;
+    while (true) {
+        if (lvl >= 254) {
+            set_error("eg_msbfs: more than 254 levels");
+            return EG_ERR_UNSUPPORTED;
+        }
+        EG_CUDA(cudaMemsetAsync(next, 0, 8 * V, g->stream));
+        EG_CUDA(cudaMemsetAsync(d_new, 0, 4, g->stream));
+        MsBfsPullOp op{front, visit, next, lev, lvl + 1, full, d_new, d_reach, g->outdeg.as<uint32_t>()};
+        EG_TRY(launch_pull(g, op, "msbfs_pull"));
+        ++sweeps;
+        uint32_t h = 0;
+        EG_CUDA(cudaMemcpyAsync(&h, d_new, 4, cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaStreamSynchronize(g->stream));
+        if (!h) break;
+        std::swap(front, next);
+        ++lvl;
+    }
+    if (levels) {
+        uint8_t* out = levels;
+        if (where != EG_DEVICE) {
+            EG_TRY(b.tmp_out.reserve((size_t)n * V + 64));
+            out = b.tmp_out.as<uint8_t>();
+        }
+        dim3 blk(32, 8);
+        k_transpose_u8<<<(unsigned)((V + 31) / 32), blk, 0, g->stream>>>(lev, (uint32_t)V, n, out);
+        EG_CHECK_LAUNCH("k_transpose_u8");
+        if (where != EG_DEVICE)
+            EG_CUDA(cudaMemcpyAsync(levels, out, (size_t)n * V, cudaMemcpyDeviceToHost, g->stream));
+    }
+    unsigned long long reach = 0;
+    EG_CUDA(cudaMemcpyAsync(&reach, d_reach, 8, cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    if (edges) *edges = reach;
+    g->last_edges_processed = reach;
+    g->last_iterations = sweeps;
+    g->last_pushes = 0;
+    g->last_pulls = sweeps;
+    return EG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+static int ensure_tasks(eg_graph* g, bool csr) {
+    BatchState& b = bstate(g);
+    if (csr) {
+        if (!b.csr_ready) {
+            EG_TRY(make_tasks(g, b.csr_tasks, g->csr_off.as<uint64_t>(), g->V));
+            b.csr_ready = true;
+        }
+    } else if (!b.csc_ready) {
+        EG_TRY(make_tasks(g, b.csc_tasks, g->cidx.as<uint64_t>(), g->ncompressed - 1));
+        b.csc_ready = true;
+    }
+    return EG_OK;
+}
+
+static unsigned row_grid(eg_graph* g) { return (unsigned)g->num_sms * 8u; }
+
+static RowArgs row_args(const RowTasks& t, const uint32_t* item_vertex, const uint32_t* adj, const float* w) {
+    RowArgs a;
+    a.t_item = t.item.as<uint32_t>();
+    a.t_part = t.part.as<uint32_t>();
+    a.ntasks = t.ntasks;
+    a.heavy_slot = t.heavy_slot.as<uint32_t>();
+    a.item_vertex = item_vertex;
+    a.begin = t.begin;
+    a.adj = adj;
+    a.w = w;
+    return a;
+}
+
+// weights in CSR and CSC order, row-normalised by the source's out-weight sum
+static int prepare_ppr_weights(eg_graph* g, const float* w_in_dev) {
+    BatchState& b = bstate(g);
+    const uint64_t E = g->E, V = g->V;
+    EG_TRY(b.wn_csc.reserve(4 * E + 64));
+    EG_TRY(b.wn_csr.reserve(4 * E + 64));
+    EG_TRY(b.s_out.reserve(4 * V + 64));
+    EG_TRY(b.row_of.reserve(4 * E + 64));
+    const unsigned gv = grid_for(V, 256, 152u * 16u), ge = grid_for(E, 256, 152u * 16u);
+    Timed t(&g->prof, g->stream, "ppr_weights");
+    k_out_weight_sums<<<gv, 256, 0, g->stream>>>(g->csr_off.as<uint64_t>(), g->csr_w.as<float>(), w_in_dev, (uint32_t)V,
+                                                 b.s_out.as<float>());
+    EG_CHECK_LAUNCH("k_out_weight_sums");
+    // CSC: the neighbour is the source
+    k_gather_norm_w<<<ge, 256, 0, g->stream>>>(g->csc_adj.as<uint32_t>(), g->csc_w.as<float>(), w_in_dev,
+                                               b.s_out.as<float>(), E, b.wn_csc.as<float>());
+    EG_CHECK_LAUNCH("k_gather_norm_w");
+    // CSR: the source is the row
+    k_row_of<<<gv, 256, 0, g->stream>>>(g->csr_off.as<uint64_t>(), (uint32_t)V, b.row_of.as<uint32_t>());
+    EG_CHECK_LAUNCH("k_row_of");
+    k_gather_norm_w<<<ge, 256, 0, g->stream>>>(b.row_of.as<uint32_t>(), g->csr_w.as<float>(), w_in_dev,
+                                               b.s_out.as<float>(), E, b.wn_csr.as<float>());
+    EG_CHECK_LAUNCH("k_gather_norm_w");
+    return EG_OK;
+}
+
+// one forward step: y = a*e + (1-a) A^T x
+static int ppr_step(eg_graph* g, const float* x, float* y, float alpha, int n) {
+    BatchState& b = bstate(g);
+    const uint64_t V = g->V;
+    const RowTasks& t = b.csc_tasks;
+    EG_CUDA(cudaMemsetAsync(y, 0, 256 * V, g->stream));
+    RowArgs a = row_args(t, g->cvert.as<uint32_t>(), g->csc_adj.as<uint32_t>(), b.wn_csc.as<float>());
+    Timed tm(&g->prof, g->stream, "ppr_spmm");
+    k_row_spmm<<<row_grid(g), 256, 0, g->stream>>>(a, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(y),
+                                                  b.heavy.as<float2>(), 1.0f - alpha);
+    EG_CHECK_LAUNCH("k_row_spmm");
+    if (t.nheavy) {
+        k_row_heavy_finish<<<(unsigned)((t.nheavy * 32ull + 255) / 256), 256, 0, g->stream>>>(
+            t.heavy_item.as<uint32_t>(), g->cvert.as<uint32_t>(), t.nheavy, b.heavy.as<float2>(),
+            reinterpret_cast<float2*>(y), 1.0f - alpha);
+        EG_CHECK_LAUNCH("k_row_heavy_finish");
+    }
+    k_ppr_teleport<<<1, 64, 0, g->stream>>>(b.seeds.as<uint32_t>(), n, y, alpha);
+    EG_CHECK_LAUNCH("k_ppr_teleport");
+    return EG_OK;
+}
+
+static int ppr_common(eg_graph* g, const float* w_in, const uint32_t* seeds, int n, float alpha, int K, int where,
+                      const float** w_dev) {
+    if (!g->built_csc || !g->built_csr) { set_error("eg_ppr: graph not built"); return EG_ERR_STATE; }
+    if (!g->weighted || !g->edge_ids) {
+        set_error("eg_ppr: load the graph with eg_load_directed_with_ids (per-edge ids select the weights)");
+        return EG_ERR_STATE;
+    }
+    if (!w_in || K < 0 || !(alpha > 0.f && alpha <= 1.f)) { set_error("eg_ppr: need weights, K >= 0, 0 < alpha <= 1"); return EG_ERR_INVALID; }
+    EG_TRY(check_roots(g, seeds, n, where, "eg_ppr"));
+    BatchState& b = bstate(g);
+    const uint64_t V = g->V, E = g->E_input;
+    EG_TRY(copy_small_in(g, b.seeds, seeds, n, where));
+    const float* wd = w_in;
+    if (where != EG_DEVICE) {
+        EG_TRY(b.tmp_out.reserve(4 * E + 64));
+        EG_CUDA(cudaMemcpyAsync(b.tmp_out.ptr, w_in, 4 * E, cudaMemcpyHostToDevice, g->stream));
+        wd = b.tmp_out.as<float>();
+    }
+    *w_dev = wd;
+    EG_TRY(ensure_tasks(g, false));
+    EG_TRY(ensure_tasks(g, true));
+    EG_TRY(b.heavy.reserve(256ull * (std::max(b.csc_tasks.nheavy, b.csr_tasks.nheavy) + 1)));
+    EG_CUDA(cudaMemsetAsync(b.heavy.ptr, 0, b.heavy.bytes, g->stream));
+    EG_TRY(b.rows0.reserve(256 * V + 256));
+    EG_TRY(b.rows1.reserve(256 * V + 256));
+    return prepare_ppr_weights(g, wd);
+}
+
+int run_ppr(eg_graph* g, const float* w_in, const uint32_t* seeds, int n, float alpha, int K, float* out, int where) {
+    const float* wd = nullptr;
+    EG_TRY(ppr_common(g, w_in, seeds, n, alpha, K, where, &wd));
+    BatchState& b = bstate(g);
+    const uint64_t V = g->V;
+    float* x = b.rows0.as<float>();
+    float* y = b.rows1.as<float>();
+    EG_CUDA(cudaMemsetAsync(x, 0, 256 * V, g->stream));
+    k_ppr_init<<<1, 64, 0, g->stream>>>(b.seeds.as<uint32_t>(), n, x);
+    EG_CHECK_LAUNCH("k_ppr_init");
+    for (int k = 0; k < K; ++k) {
+        EG_TRY(ppr_step(g, x, y, alpha, n));
+        std::swap(x, y);
+    }
+    if (out) {
+        float* dst = out;
+        if (where != EG_DEVICE) {
+            EG_TRY(b.tmp_out.reserve(4ull * n * V + 64));
+            dst = b.tmp_out.as<float>();
+        }
+        dim3 blk(32, 8);
+        k_transpose_rows<float><<<(unsigned)((V + 31) / 32), blk, 0, g->stream>>>(x, (uint32_t)V, n, dst);
+        EG_CHECK_LAUNCH("k_transpose_rows");
+        if (where != EG_DEVICE) EG_CUDA(cudaMemcpyAsync(out, dst, 4ull * n * V, cudaMemcpyDeviceToHost, g->stream));
+    }
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    g->last_edges_processed = g->E * (uint64_t)K;
+    g->last_iterations = K;
+    return EG_OK;
+}
+
+// adjoint of K forward steps from x_0 = e_seed; dL/dx_K given as [n][V]; dL/dw in input edge order
+int run_ppr_backward(eg_graph* g, const float* w_in, const uint32_t* seeds, int n, float alpha, int K,
+                     const float* dl_dx, float* dl_dw, int where) {
+    const float* wd = nullptr;
+    EG_TRY(ppr_common(g, w_in, seeds, n, alpha, K, where, &wd));
+    if (!dl_dx || !dl_dw) { set_error("eg_ppr_backward: need dL/dx and the dL/dw output"); return EG_ERR_INVALID; }
+    BatchState& b = bstate(g);
+    const uint64_t V = g->V, E = g->E, Ein = g->E_input;
+    const int C = std::max(1, (int)ceil(sqrt((double)std::max(K, 1))));  // checkpoint stride
+    const int ncp = K / C + 1;
+    const size_t row = 256 * V;
+    EG_TRY(b.ck.reserve(row * ncp + 256));
+    EG_TRY(b.seg.reserve(row * (C + 1) + 256));
+    EG_TRY(b.gA.reserve(4 * E + 64));
+    // forward with checkpoints x_0, x_C, x_2C, ...
+    float* ck = b.ck.as<float>();
+    EG_CUDA(cudaMemsetAsync(ck, 0, row, g->stream));
+    k_ppr_init<<<1, 64, 0, g->stream>>>(b.seeds.as<uint32_t>(), n, ck);
+    EG_CHECK_LAUNCH("k_ppr_init");
+    {
+        float* x = b.rows0.as<float>();
+        float* y = b.rows1.as<float>();
+        EG_CUDA(cudaMemcpyAsync(x, ck, row, cudaMemcpyDeviceToDevice, g->stream));
+        for (int k = 0; k < K; ++k) {
+            EG_TRY(ppr_step(g, x, y, alpha, n));
+            std::swap(x, y);
+            if ((k + 1) % C == 0 && (k + 1) / C < ncp)
+                EG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(ck) + row * ((k + 1) / C), x, row, cudaMemcpyDeviceToDevice,
+                                        g->stream));
+        }
+    }
+    // lambda_K from dL/dx_K ([n][V] -> [V][64])
+    float* lam = b.rows0.as<float>();
+    float* lam2 = b.rows1.as<float>();
+    {
+        const float* src = dl_dx;
+        if (where != EG_DEVICE) {
+            EG_TRY(b.tmp_out.reserve(4ull * n * V + 64));
+            EG_CUDA(cudaMemcpyAsync(b.tmp_out.ptr, dl_dx, 4ull * n * V, cudaMemcpyHostToDevice, g->stream));
+            src = b.tmp_out.as<float>();
+        }
+        dim3 blk(32, 8);
+        k_untranspose_rows<float><<<(unsigned)((V + 31) / 32), blk, 0, g->stream>>>(src, (uint32_t)V, n, lam);
+        EG_CHECK_LAUNCH("k_untranspose_rows");
+    }
+    EG_CUDA(cudaMemsetAsync(b.gA.ptr, 0, 4 * E, g->stream));
+    const RowTasks& tr = b.csr_tasks;
+    RowArgs ar = row_args(tr, nullptr, g->csr_adj.as<uint32_t>(), b.wn_csr.as<float>());
+    float* seg = b.seg.as<float>();
+    for (int cp = (K - 1) / C; cp >= 0 && K > 0; --cp) {
+        const int k0 = cp * C, k1 = std::min(K, k0 + C);
+        // recompute x_k0 .. x_{k1-1} into the segment buffer
+        EG_CUDA(cudaMemcpyAsync(seg, reinterpret_cast<char*>(ck) + row * cp, row, cudaMemcpyDeviceToDevice, g->stream));
+        for (int k = k0 + 1; k < k1; ++k)
+            EG_TRY(ppr_step(g, seg + (size_t)(k - 1 - k0) * 64 * V, seg + (size_t)(k - k0) * 64 * V, alpha, n));
+        for (int k = k1 - 1; k >= k0; --k) {
+            // lam holds lambda_{k+1}; gA += (1-a) <x_k[u], lam[v]>; lam2 = (1-a) A lam
+            EG_CUDA(cudaMemsetAsync(lam2, 0, row, g->stream));
+            {
+                Timed tm(&g->prof, g->stream, "ppr_adjoint");
+                k_row_adjoint<<<row_grid(g), 256, 0, g->stream>>>(
+                    ar, reinterpret_cast<const float2*>(lam), reinterpret_cast<const float2*>(seg + (size_t)(k - k0) * 64 * V),
+                    reinterpret_cast<float2*>(lam2), b.heavy.as<float2>(), b.gA.as<float>(), 1.0f - alpha);
+                EG_CHECK_LAUNCH("k_row_adjoint");
+            }
+            if (tr.nheavy) {
+                k_row_heavy_finish<<<(unsigned)((tr.nheavy * 32ull + 255) / 256), 256, 0, g->stream>>>(
+                    tr.heavy_item.as<uint32_t>(), nullptr, tr.nheavy, b.heavy.as<float2>(), reinterpret_cast<float2*>(lam2),
+                    1.0f - alpha);
+                EG_CHECK_LAUNCH("k_row_heavy_finish");
+            }
+            std::swap(lam, lam2);
+        }
+    }
+    // dL/dw
+    float* dw = dl_dw;
+    if (where != EG_DEVICE) {
+        EG_TRY(b.tmp_out.reserve(4 * Ein + 64));
+        dw = b.tmp_out.as<float>();
+    }
+    EG_CUDA(cudaMemsetAsync(dw, 0, 4 * Ein, g->stream));
+    k_weight_grad<<<grid_for(V, 256, 152u * 16u), 256, 0, g->stream>>>(g->csr_off.as<uint64_t>(), (uint32_t)V,
+                                                                       b.wn_csr.as<float>(), b.gA.as<float>(),
+                                                                       b.s_out.as<float>(), g->csr_w.as<float>(), dw);
+    EG_CHECK_LAUNCH("k_weight_grad");
+    if (where != EG_DEVICE) EG_CUDA(cudaMemcpyAsync(dl_dw, dw, 4 * Ein, cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    return EG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+int run_sssp_batch(eg_graph* g, const uint32_t* srcs, int n, float* out, int where) {
+    if (!g->built_csc) { set_error("eg_sssp_batch: CSC not built"); return EG_ERR_STATE; }
+    if (!g->weighted || g->edge_ids) { set_error("eg_sssp_batch: graph needs float edge weights"); return EG_ERR_STATE; }
+    EG_TRY(check_roots(g, srcs, n, where, "eg_sssp_batch"));
+    EG_TRY(ensure_tasks(g, false));
+    BatchState& b = bstate(g);
+    const uint64_t V = g->V;
+    EG_TRY(copy_small_in(g, b.seeds, srcs, n, where));
+    EG_TRY(b.rows0.reserve(256 * V + 256));
+    EG_TRY(b.ch0.reserve(V + 64));
+    EG_TRY(b.ch1.reserve(V + 64));
+    EG_TRY(b.flag.reserve(16));
+    float* dist = b.rows0.as<float>();
+    {
+        Timed t(&g->prof, g->stream, "sssp_batch_init");
+        k_fill_f32_rows<<<grid_for(64 * V, 256, 152u * 16u), 256, 0, g->stream>>>(dist, 64 * V, 1e9f);
+        EG_CHECK_LAUNCH("k_fill_f32_rows");
+        EG_CUDA(cudaMemsetAsync(b.ch0.ptr, 0, V, g->stream));
+        k_sssp_batch_init<<<1, 64, 0, g->stream>>>(b.seeds.as<uint32_t>(), n, dist, b.ch0.as<uint8_t>());
+        EG_CHECK_LAUNCH("k_sssp_batch_init");
+    }
+    RowArgs a = row_args(b.csc_tasks, g->cvert.as<uint32_t>(), g->csc_adj.as<uint32_t>(), g->csc_w.as<float>());
+    uint8_t* prev = b.ch0.as<uint8_t>();
+    uint8_t* nxt = b.ch1.as<uint8_t>();
+    int sweeps = 0;
+    while (true) {
+        EG_CUDA(cudaMemsetAsync(nxt, 0, V, g->stream));
+        EG_CUDA(cudaMemsetAsync(b.flag.ptr, 0, 4, g->stream));
+        {
+            Timed t(&g->prof, g->stream, "sssp_batch_sweep");
+            k_row_sssp<<<row_grid(g), 256, 0, g->stream>>>(a, reinterpret_cast<float2*>(dist), prev, nxt, b.flag.as<int>());
+            EG_CHECK_LAUNCH("k_row_sssp");
+        }
+        ++sweeps;
+        int any = 0;
+        EG_CUDA(cudaMemcpyAsync(&any, b.flag.ptr, 4, cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaStreamSynchronize(g->stream));
+        if (!any) break;
+        std::swap(prev, nxt);
+    }
+    if (out) {
+        float* dst = out;
+        if (where != EG_DEVICE) {
+            EG_TRY(b.tmp_out.reserve(4ull * n * V + 64));
+            dst = b.tmp_out.as<float>();
+        }
+        dim3 blk(32, 8);
+        k_transpose_rows<float><<<(unsigned)((V + 31) / 32), blk, 0, g->stream>>>(dist, (uint32_t)V, n, dst);
+        EG_CHECK_LAUNCH("k_transpose_rows");
+        if (where != EG_DEVICE) EG_CUDA(cudaMemcpyAsync(out, dst, 4ull * n * V, cudaMemcpyDeviceToHost, g->stream));
+    }
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    g->last_iterations = sweeps;
+    g->last_pulls = sweeps;
+    g->last_pushes = 0;
+    return EG_OK;
+}
+
+}  // namespace eg

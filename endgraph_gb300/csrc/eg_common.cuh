@@ -166,6 +166,10 @@ struct eg_graph {
     // pinned staging for host inputs
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
+    // batched operators (eg_batch.cu): opaque state, dropped at every load/build
+    void* batch = nullptr;
+    bool edge_ids = false;   // the weight slot of each record holds the record's input index
+    uint64_t E_input = 0;    // records as loaded (before symmetrisation)
     // engine options (eg_set_option)
     int bfs_direction = 0;  // 0: Gemini threshold switch, 1: push only, 2: pull only
     int dense_div = 20;     // sparse iff active_edges < E / dense_div (core/graph.hpp:1491)
@@ -193,6 +197,13 @@ int run_pagerank(eg_graph* g, int iterations, float damping, float* out, int whe
 int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int where, uint64_t* reached);
 int run_sssp(eg_graph* g, uint32_t root, float* dist, int where);
 int run_cc(eg_graph* g, uint32_t* label, int where);
+int run_msbfs(eg_graph* g, const uint32_t* roots, int n, uint8_t* levels, int where, uint64_t* edges);
+int run_ppr(eg_graph* g, const float* w_in, const uint32_t* seeds, int n, float alpha, int K, float* out, int where);
+int run_ppr_backward(eg_graph* g, const float* w_in, const uint32_t* seeds, int n, float alpha, int K,
+                     const float* dl_dx, float* dl_dw, int where);
+int run_sssp_batch(eg_graph* g, const uint32_t* srcs, int n, float* out, int where);
+void free_batch_state(eg_graph* g);
+int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E);
 
 // device helpers
 __device__ __forceinline__ uint32_t part_of(const uint32_t* __restrict__ off, int P, uint32_t v) {

@@ -171,6 +171,28 @@ int eg_sssp(eg_graph* g, uint32_t root, float* dist, int where);
 enum { EG_OPT_BFS_DIRECTION = 1, EG_OPT_DENSE_DIVISOR = 2 };
 int eg_set_option(eg_graph* g, int option, int64_t value);
 
+/* ---- batched operators (no reference counterpart: batched forms of the toolkits) ---------- */
+/* Bit-parallel BFS from nroots <= 64 roots (toolkits/bfs.cpp semantics per root): levels[n][V]
+ * bytes (0xFF unreached; may be NULL), *edges = sum over roots of the out-edges of the vertices
+ * each root reaches.  Identical levels to nroots separate eg_bfs calls. */
+int eg_msbfs(eg_graph* g, const uint32_t* roots, int nroots, uint8_t* levels, int where, uint64_t* edges);
+/* Bellman-Ford from nsources <= 64 sources on a weighted graph (toolkits/sssp.cpp per source):
+ * dist[n][V] floats, 1e9 when unreachable; bit-identical to separate eg_sssp calls. */
+int eg_sssp_batch(eg_graph* g, const uint32_t* sources, int nsources, float* dist, int where);
+/* Load {src, dst} records keeping each record's input index with it, for operators that take
+ * per-edge values at call time (eg_ppr*).  Builds CPBT + CSR + CSC like eg_load_directed. */
+int eg_load_directed_with_ids(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int where);
+/* Personalised PageRank for nseeds <= 64 seeds over the learnable weights w[E] (input edge order):
+ * x_0 = e_seed, x_{k+1} = alpha e_seed + (1 - alpha) A^T x_k with A_uv = w_uv / sum_v' w_uv',
+ * FP32; out[n][V] = x_iterations.  Graph loaded with eg_load_directed_with_ids. */
+int eg_ppr(eg_graph* g, const float* weights, const uint32_t* seeds, int nseeds, float alpha, int iterations,
+           float* out, int where);
+/* Adjoint of eg_ppr: given dL/dx_iterations (dl_dx[n][V]) writes dL/dw (dl_dw[E], input edge
+ * order).  The transposed iteration runs over the CSR; iterates are recomputed from checkpoints
+ * stored every ceil(sqrt(iterations)) steps. */
+int eg_ppr_backward(eg_graph* g, const float* weights, const uint32_t* seeds, int nseeds, float alpha, int iterations,
+                    const float* dl_dx, float* dl_dw, int where);
+
 /* statistics of the last toolkit call: edges traversed, iterations, push / pull iterations */
 int eg_last_run(eg_graph* g, uint64_t* edges_processed, int* iterations, int* push_iters, int* pull_iters);
 

@@ -1,0 +1,150 @@
+"""Batched operators through the C ABI: 64-root bit-parallel BFS and 64-source SSSP against the
+oracle's single-source runs (bit-exact), personalised PageRank against an FP64 reference, and its
+adjoint against FP64 autograd (dense) and FP64 central finite differences."""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import rel_l1, rmat_graph
+
+pytestmark = pytest.mark.gpu
+
+
+def test_msbfs_matches_single_source(eg_lib):
+    import endgraph_gb300 as eg
+    V, E = 1 << 14, 1 << 18
+    src, dst, _ = rmat_graph(V, E, 91)
+    csr = oracle.build_csr(src, dst, None, V, np.array([0, V], np.uint32))
+    rng = np.random.default_rng(3)
+    roots = np.concatenate([src[rng.integers(0, E, 60)], [src[0], src[0]], rng.integers(0, V, 2)]).astype(np.uint32)
+    with eg.Graph() as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        levels, edges = g.msbfs(roots)
+        total = 0
+        deg = np.diff(csr["off"][0].astype(np.int64))
+        for s, r in enumerate(roots):
+            ref = oracle.bfs_levels(csr["off"][0], csr["adj"], V, int(r))
+            ref8 = np.where(ref == oracle.UNREACHED, 255, ref).astype(np.uint8)
+            assert np.array_equal(levels[s], ref8), s
+            total += int(deg[ref != oracle.UNREACHED].sum())
+        assert edges == total
+
+
+def test_sssp_batch_matches_single_source(eg_lib):
+    import endgraph_gb300 as eg
+    V, E = 1 << 13, 1 << 17
+    src, dst, w = rmat_graph(V, E, 92, weights=(0.0, 1.0))
+    csr = oracle.build_csr(src, dst, w, V, np.array([0, V], np.uint32))
+    sources = np.array([src[0], src[9], dst[4], 7, src[100]] + list(src[200:259]), np.uint32)
+    with eg.Graph() as g:
+        g.load_directed(eg.pack_edges(src, dst, w), V)
+        dist = g.sssp_batch(sources)
+    for s, r in enumerate(sources):
+        ref = oracle.sssp(csr["off"][0], csr["adj"], csr["w"], V, int(r))
+        assert np.array_equal(dist[s].view(np.uint32), ref.view(np.uint32)), s
+
+
+def _ppr_fp64(src, dst, w, V, seeds, alpha, K):
+    """Dense FP64 power iteration (torch, on w's device), differentiable in w."""
+    import torch
+    n = len(seeds)
+    dev = w.device
+    s_idx = torch.as_tensor(src, dtype=torch.long, device=dev)
+    d_idx = torch.as_tensor(dst, dtype=torch.long, device=dev)
+    s_out = torch.zeros(V, dtype=torch.float64, device=dev).index_add(0, s_idx, w)
+    a_val = w / s_out[s_idx]
+    e = torch.zeros(V, n, dtype=torch.float64, device=dev)
+    e[torch.as_tensor(seeds, dtype=torch.long, device=dev), torch.arange(n, device=dev)] = 1.0
+    A = torch.zeros(V, V, dtype=torch.float64, device=dev).index_put((s_idx, d_idx), a_val, accumulate=True)
+    x = e.clone()
+    for _ in range(K):
+        x = alpha * e + (1 - alpha) * (A.T @ x)
+    return x.T  # [n][V]
+
+
+def _small_graph(V, E, seed):
+    src, dst, _ = rmat_graph(V, E, seed)
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(0.5, 1.5, E).astype(np.float32)  # U[0.5, 1.5)
+    return src, dst, w
+
+
+def test_ppr_forward_fp64(eg_lib):
+    import torch
+    import endgraph_gb300 as eg
+    V, E, K, alpha = 1024, 16384, 50, 0.15
+    src, dst, w = _small_graph(V, E, 93)
+    seeds = np.array(src[:64], np.uint32)
+    with eg.Graph() as g:
+        g.load_directed_with_ids(eg.pack_edges(src, dst), V)
+        x = g.ppr(w, seeds, alpha, K)
+    ref = _ppr_fp64(src, dst, torch.as_tensor(w, dtype=torch.float64), V, seeds, alpha, K).numpy()
+    assert rel_l1(x, ref) <= 1e-6, rel_l1(x, ref)
+
+
+class _PPR:
+    """torch.autograd.Function over the C-ABI forward / backward (test harness only)."""
+
+    @staticmethod
+    def make(g, seeds, alpha, K):
+        import torch
+
+        class F(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, w):
+                ctx.save_for_backward(w)
+                out = torch.empty((len(seeds), g.info().V), dtype=torch.float32, device=w.device)
+                g.ppr(w, seeds, alpha, K, out=out)
+                return out
+
+            @staticmethod
+            def backward(ctx, grad_out):
+                (w,) = ctx.saved_tensors
+                dw = torch.empty_like(w)
+                g.ppr_backward(w, seeds, grad_out.contiguous(), alpha, K, dl_dw=dw)
+                return dw
+
+        return F
+
+
+def test_ppr_adjoint_against_fp64_autograd_and_finite_differences(eg_lib):
+    import torch
+    import endgraph_gb300 as eg
+    V, E, K, alpha = 1024, 8192, 50, 0.15
+    src, dst, w = _small_graph(V, E, 94)
+    seeds = np.array(src[:64], np.uint32)
+    rng = np.random.default_rng(5)
+    target = rng.random((64, V)) * 2.0 / V
+    with eg.Graph() as g:
+        g.load_directed_with_ids(eg.pack_edges(src, dst), V)
+        F = _PPR.make(g, seeds, alpha, K)
+        wt = torch.tensor(w, device="cuda", requires_grad=True)
+        x = F.apply(wt)
+        loss = ((x - torch.as_tensor(target, dtype=torch.float32, device="cuda")) ** 2).sum()
+        loss.backward()
+        grad = wt.grad.cpu().numpy().astype(np.float64)
+    # dense FP64 reference gradient
+    w64 = torch.tensor(w, dtype=torch.float64, requires_grad=True)
+    x64 = _ppr_fp64(src, dst, w64, V, seeds, alpha, K)
+    l64 = ((x64 - torch.as_tensor(target)) ** 2).sum()
+    l64.backward()
+    g64 = w64.grad.numpy()
+    rel = np.linalg.norm(grad - g64) / np.linalg.norm(g64)
+    assert rel <= 1e-4, rel
+    # FP64 central finite differences on 256 random edges
+    idx = rng.choice(E, 256, replace=False)
+    h = 1e-6
+    fd = np.empty(256)
+    with torch.no_grad():
+        base = torch.tensor(w, dtype=torch.float64, device="cuda")
+        tgt = torch.as_tensor(target, device="cuda")
+        for j, i in enumerate(idx):
+            wp = base.clone()
+            wp[i] += h
+            wm = base.clone()
+            wm[i] -= h
+            lp = ((_ppr_fp64(src, dst, wp, V, seeds, alpha, K) - tgt) ** 2).sum().item()
+            lm = ((_ppr_fp64(src, dst, wm, V, seeds, alpha, K) - tgt) ** 2).sum().item()
+            fd[j] = (lp - lm) / (2 * h)
+    err = np.linalg.norm(grad[idx] - fd) / np.linalg.norm(fd)
+    assert err <= 1e-3, err
