@@ -45,6 +45,8 @@ def parse_args():
     p.add_argument("--seed", type=int, default=20240601)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--ppr-scale", type=int, default=22)
     return p.parse_args()
 
 
@@ -197,6 +199,78 @@ ALG_BYTES = {  # algorithmic bytes per launch (E edges, V vertices, nc compresse
 }
 
 
+def _timed(stream, fn):
+    import torch
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    out = fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b), out
+
+
+def run_batched(args, g, edges, roots, dev, stream):
+    """64-root bit-parallel BFS vs 64 single-root BFS on the bench graph; 64-seed personalised
+    PageRank (+ adjoint) vs 64 single-seed runs on R-MAT 2^ppr_scale x 16 with U[0.5,1.5) weights."""
+    import numpy as np
+    import torch
+
+    import endgraph_gb300 as eg
+    V = g.info().V
+    res = {}
+    level = torch.empty(V, dtype=torch.int32, device=dev)
+    lev64 = torch.empty((64, V), dtype=torch.uint8, device=dev)
+
+    def plain_bfs():
+        tot = 0
+        for r in roots:
+            g.bfs(r, level=level, want_parent=False)
+            tot += g.last_run()["edges"]
+        return tot
+
+    plain_bfs()  # warm
+    t_plain, e_plain = _timed(stream, plain_bfs)
+    g.msbfs(roots, levels=lev64)
+    t_ms, (_, e_ms) = _timed(stream, lambda: g.msbfs(roots, levels=lev64))
+    res["msbfs64"] = {"roots": 64, "plain_ms": round(t_plain, 3), "batched_ms": round(t_ms, 3),
+                      "plain_gteps": round(e_plain / t_plain / 1e6, 2), "batched_gteps": round(e_ms / t_ms / 1e6, 2),
+                      "speedup": round(t_plain / t_ms, 2), "same_edges": e_plain == e_ms,
+                      "sweeps": g.last_run()["iterations"]}
+    # personalised PageRank workload
+    Vp = 1 << args.ppr_scale
+    Ep = Vp * 16
+    ep = torch.empty((Ep, 2), dtype=torch.int32, device=dev)
+    eg.generate_rmat(ep, Vp, Ep, args.seed + 7, 0.57, 0.19, 0.19, permute=True)
+    w = (torch.rand(Ep, generator=torch.Generator(device="cpu").manual_seed(args.seed), dtype=torch.float32) + 0.5).to(dev)
+    seeds = ep[:64, 0].cpu().numpy().view(np.uint32).copy()
+    K = 50
+    with eg.Graph(eta=1, device=dev.index or 0) as gp:
+        gp.load_directed_with_ids(ep, Vp)
+        s2 = torch.cuda.ExternalStream(gp.stream, device=dev)
+        x1 = torch.empty((1, Vp), dtype=torch.float32, device=dev)
+        x64 = torch.empty((64, Vp), dtype=torch.float32, device=dev)
+        gp.ppr(w, seeds[:1], 0.15, K, out=x1)
+
+        def plain_ppr():
+            for s in seeds:
+                gp.ppr(w, np.array([s], np.uint32), 0.15, K, out=x1)
+
+        t_plain, _ = _timed(s2, plain_ppr)
+        gp.ppr(w, seeds, 0.15, K, out=x64)
+        t_b, _ = _timed(s2, lambda: gp.ppr(w, seeds, 0.15, K, out=x64))
+        dl = torch.randn((64, Vp), dtype=torch.float32, device=dev) * 1e-3
+        dw = torch.empty_like(w)
+        gp.ppr_backward(w, seeds, dl, 0.15, K, dl_dw=dw)
+        t_bw, _ = _timed(s2, lambda: gp.ppr_backward(w, seeds, dl, 0.15, K, dl_dw=dw))
+        res["ppr64"] = {"V": Vp, "E": Ep, "seeds": 64, "iterations": K, "alpha": 0.15,
+                        "plain_ms": round(t_plain, 3), "batched_ms": round(t_b, 3),
+                        "plain_gteps": round(64 * K * Ep / t_plain / 1e6, 2),
+                        "batched_gteps": round(64 * K * Ep / t_b / 1e6, 2), "speedup": round(t_plain / t_b, 2),
+                        "adjoint_ms": round(t_bw, 3)}
+    return res
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -214,8 +288,9 @@ def run_ours(args, world, rank, local):
     eg.generate_rmat(edges, V, E, seed, A, B, C, permute=True)
     torch.cuda.synchronize()
     gen = torch.Generator(device="cpu").manual_seed(seed)
-    ridx = torch.randint(0, E, (args.roots,), generator=gen)
-    roots = [int(x) for x in edges[ridx.to(dev), 0].cpu().numpy().view(np.uint32)]
+    ridx = torch.randint(0, E, (64,), generator=gen)
+    roots_all = [int(x) for x in edges[ridx.to(dev), 0].cpu().numpy().view(np.uint32)]
+    roots = roots_all[:args.roots]
 
     g = eg.Graph(eta=1, partitions=1, max_iterations=args.pr_iters, device=local)
     g.load_edges(edges, V)
@@ -321,6 +396,8 @@ def run_ours(args, world, rank, local):
         g2.close()
         del host
 
+    batched = None if args.no_batched else run_batched(args, g, edges, roots_all, dev, stream)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sv, se = V >> 3, E >> 3
@@ -356,6 +433,7 @@ def run_ours(args, world, rank, local):
                          "frac": None if achieved is None else round(achieved / peak, 4),
                          "traffic": traffic, "peak_kind": peak_kind},
             "kernels": kernels,
+            "batched": batched,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,

@@ -635,11 +635,87 @@ static int ppr_common(eg_graph* g, const float* w_in, const uint32_t* seeds, int
     return prepare_ppr_weights(g, wd);
 }
 
+// one seed: the scalar chunked pull (4-byte gathers of x[src] times the normalised weight)
+struct PprPullOp {
+    using Acc = float;
+    static constexpr bool kFilter = false;
+    __device__ bool item_active(uint32_t) const { return true; }
+    const float* x;
+    const float* wn;
+    float* y;
+    float* acc;
+    float scale;
+    __device__ Acc identity() const { return 0.f; }
+    __device__ Acc gather(uint32_t u, uint64_t e) const { return __ldcg(x + u) * __ldg(wn + e); }
+    __device__ Acc combine(Acc a, Acc b) const { return a + b; }
+    __device__ void smem_add(Acc* slot, Acc v) const { atomicAdd(slot, v); }
+    __device__ void finish(bool ok, uint32_t v, Acc a, bool whole) const {
+        if (!ok) return;
+        if (whole) y[v] = scale * a;
+        else atomicAdd(acc + v, a);
+    }
+};
+
+__global__ void k_ppr_split(const uint32_t* __restrict__ split, const uint32_t* __restrict__ cvert, uint64_t nsplit,
+                            float* y, float* acc, float scale) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nsplit; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = cvert[split[i]];
+        y[v] = scale * acc[v];
+        acc[v] = 0.f;
+    }
+}
+
+__global__ void k_ppr_seed1(uint32_t seed, float* y, float value, int add) {
+    if (add) y[seed] += value;
+    else y[seed] = value;
+}
+
+static int run_ppr_single(eg_graph* g, uint32_t seed, float alpha, int K, float* out, int where) {
+    BatchState& b = bstate(g);
+    EngineState& s = g->eng;
+    const uint64_t V = g->V;
+    EG_TRY(ensure_engine(g));
+    EG_TRY(setup_pull(g));
+    float* x = s.vals0.as<float>();
+    float* y = s.vals1.as<float>();
+    EG_CUDA(cudaMemsetAsync(x, 0, 4 * V, g->stream));
+    EG_CUDA(cudaMemsetAsync(s.acc.ptr, 0, 4 * V, g->stream));
+    k_ppr_seed1<<<1, 1, 0, g->stream>>>(seed, x, 1.0f, 0);
+    EG_CHECK_LAUNCH("k_ppr_seed1");
+    for (int k = 0; k < K; ++k) {
+        EG_CUDA(cudaMemsetAsync(y, 0, 4 * V, g->stream));
+        // single = true: whole items write y directly, split items go through acc
+        PprPullOp op{x, b.wn_csc.as<float>(), y, s.acc.as<float>(), 1.0f - alpha};
+        EG_TRY(launch_pull(g, op, "ppr1_pull"));
+        if (s.pull_nsplit) {
+            k_ppr_split<<<grid_for(s.pull_nsplit, 256), 256, 0, g->stream>>>(s.pull_split.as<uint32_t>(), g->cvert.as<uint32_t>(),
+                                                                             s.pull_nsplit, y, s.acc.as<float>(), 1.0f - alpha);
+            EG_CHECK_LAUNCH("k_ppr_split");
+        }
+        k_ppr_seed1<<<1, 1, 0, g->stream>>>(seed, y, alpha, 1);
+        EG_CHECK_LAUNCH("k_ppr_seed1");
+        std::swap(x, y);
+    }
+    if (out)
+        EG_CUDA(cudaMemcpyAsync(out, x, 4 * V, where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    g->last_edges_processed = g->E * (uint64_t)K;
+    g->last_iterations = K;
+    return EG_OK;
+}
+
 int run_ppr(eg_graph* g, const float* w_in, const uint32_t* seeds, int n, float alpha, int K, float* out, int where) {
     const float* wd = nullptr;
     EG_TRY(ppr_common(g, w_in, seeds, n, alpha, K, where, &wd));
     BatchState& b = bstate(g);
     const uint64_t V = g->V;
+    if (n == 1 && g->partitions == 1) {
+        uint32_t seed = 0;
+        EG_CUDA(cudaMemcpyAsync(&seed, b.seeds.ptr, 4, cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaStreamSynchronize(g->stream));
+        return run_ppr_single(g, seed, alpha, K, out, where);
+    }
     float* x = b.rows0.as<float>();
     float* y = b.rows1.as<float>();
     EG_CUDA(cudaMemsetAsync(x, 0, 256 * V, g->stream));

@@ -82,6 +82,23 @@ def test_ppr_forward_fp64(eg_lib):
     assert rel_l1(x, ref) <= 1e-6, rel_l1(x, ref)
 
 
+def test_ppr_single_seed_path(eg_lib):
+    """One seed takes the scalar pull path; it must agree with FP64 and with the 64-column engine."""
+    import torch
+    import endgraph_gb300 as eg
+    V, E, K, alpha = 1 << 14, 1 << 18, 50, 0.15
+    src, dst, w = _small_graph(V, E, 95)
+    seeds = np.array(src[:8], np.uint32)
+    with eg.Graph() as g:
+        g.load_directed_with_ids(eg.pack_edges(src, dst), V)
+        xb = g.ppr(w, seeds, alpha, K)
+        for i, s in enumerate(seeds):
+            x1 = g.ppr(w, np.array([s], np.uint32), alpha, K)
+            assert rel_l1(x1[0], xb[i]) <= 1e-6
+    ref = _ppr_fp64(src, dst, torch.as_tensor(w, dtype=torch.float64, device="cuda"), V, seeds[:2], alpha, K)
+    assert rel_l1(xb[:2], ref.cpu().numpy()) <= 1e-6
+
+
 class _PPR:
     """torch.autograd.Function over the C-ABI forward / backward (test harness only)."""
 
