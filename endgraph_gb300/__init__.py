@@ -21,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = _build.LIB
 
 EG_HOST, EG_DEVICE = 0, 1
-EG_OPT_BFS_DIRECTION, EG_OPT_DENSE_DIVISOR = 1, 2
+EG_OPT_BFS_DIRECTION, EG_OPT_DENSE_DIVISOR, EG_OPT_CUDA_GRAPH = 1, 2, 3
 STATUS = {0: "EG_OK", 1: "EG_ERR_INVALID", 2: "EG_ERR_CUDA", 3: "EG_ERR_NOMEM", 4: "EG_ERR_STATE",
           5: "EG_ERR_TIMEOUT", 6: "EG_ERR_HOST_CALLBACK", 7: "EG_ERR_UNSUPPORTED"}
 
@@ -83,6 +83,10 @@ SIGNATURES = {
     "eg_load_directed_with_ids": ([_vp, _vp, _u64, _u32, _i32], _i32),
     "eg_ppr": ([_vp, _vp, _vp, _i32, _f32, _i32, _vp, _i32], _i32),
     "eg_ppr_backward": ([_vp, _vp, _vp, _i32, _f32, _i32, _vp, _vp, _i32], _i32),
+    "eg_load_graph_batch": ([_vp, _vp, _i32, _vp, _vp, _i32, _i32], _i32),
+    "eg_get_graph_batch": ([_vp, _vp, _vp], _i32),
+    "eg_msbfs_graphs": ([_vp, _vp, _i32, _vp, _i32, _vp], _i32),
+    "eg_sssp_graphs": ([_vp, _vp, _i32, _vp, _i32], _i32),
     "eg_generate_rmat": ([_vp, _i32, _u64, _u32, _f64, _f64, _f64, _u64, _i32, _f32, _f32, _vp], _i32),
     "eg_profile_enable": ([_vp, _i32], _i32),
     "eg_profile_reset": ([_vp], _i32),
@@ -354,6 +358,41 @@ class Graph:
         _check(self._L.eg_ppr_backward(self.h, wp, sp, len(seeds), alpha, iterations, _buf(dl_dx)[0], _buf(dl_dw)[0],
                                        where))
         return dl_dw
+
+    def load_graph_batch(self, edges, graph_edges, graph_vertices):
+        """edges: all graphs' records back to back; graph_edges[G+1]; graph_vertices[G]."""
+        edges, E, rec = self._records(edges)
+        p, where = _buf(edges)
+        ge = np.ascontiguousarray(graph_edges, np.uint64)
+        gv = np.ascontiguousarray(graph_vertices, np.uint32)
+        _check(self._L.eg_load_graph_batch(self.h, p, rec, _buf(ge)[0], _buf(gv)[0], len(gv), where))
+        self._batch_G = len(gv)
+
+    def graph_batch(self):
+        G = self._batch_G
+        vo = np.empty(G + 1, np.uint64)
+        eo = np.empty(G + 1, np.uint64)
+        _check(self._L.eg_get_graph_batch(self.h, _buf(vo)[0], _buf(eo)[0]))
+        return vo, eo
+
+    def msbfs_graphs(self, roots, per_graph, levels=None):
+        roots = np.ascontiguousarray(roots, np.uint32)
+        if levels is None:
+            levels = np.empty((self.info().V, 64), np.uint8)
+        p, where = _buf(levels)
+        rp = _buf(roots)[0] if where == EG_HOST else _buf(_to_device_u32(roots, levels))[0]
+        e = ctypes.c_uint64()
+        _check(self._L.eg_msbfs_graphs(self.h, rp, per_graph, p, where, ctypes.byref(e)))
+        return levels, e.value
+
+    def sssp_graphs(self, sources, per_graph, dist=None):
+        sources = np.ascontiguousarray(sources, np.uint32)
+        if dist is None:
+            dist = np.empty((self.info().V, 64), np.float32)
+        p, where = _buf(dist)
+        sp = _buf(sources)[0] if where == EG_HOST else _buf(_to_device_u32(sources, dist))[0]
+        _check(self._L.eg_sssp_graphs(self.h, sp, per_graph, p, where))
+        return dist
 
     def set_option(self, option, value):
         _check(self._L.eg_set_option(self.h, option, value))

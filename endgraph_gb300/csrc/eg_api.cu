@@ -115,6 +115,42 @@ int eg_sync(eg_graph* g) {
 
 int eg_load_edges(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int symmetric, int where) {
     EG_TRY(check_graph(g, "eg_load_edges"));
+    return load_edges_impl(g, edges, E, V, edge_bytes, symmetric, where, true);
+}
+
+int eg_load_graph_batch(eg_graph* g, const void* edges, int edge_bytes, const uint64_t* graph_edges,
+                        const uint32_t* graph_vertices, int ngraphs, int where) {
+    EG_TRY(check_graph(g, "eg_load_graph_batch"));
+    return load_graph_batch(g, edges, edge_bytes, graph_edges, graph_vertices, ngraphs, where);
+}
+
+int eg_get_graph_batch(eg_graph* g, uint64_t* vertex_offsets, uint64_t* edge_offsets) {
+    EG_TRY(check_graph(g, "eg_get_graph_batch"));
+    if (g->batch_voff.empty()) {
+        set_error("eg_get_graph_batch: no graph batch loaded");
+        return EG_ERR_STATE;
+    }
+    if (vertex_offsets) memcpy(vertex_offsets, g->batch_voff.data(), 8 * g->batch_voff.size());
+    if (edge_offsets) memcpy(edge_offsets, g->batch_eoff.data(), 8 * g->batch_eoff.size());
+    return EG_OK;
+}
+
+int eg_msbfs_graphs(eg_graph* g, const uint32_t* roots, int roots_per_graph, uint8_t* levels, int where,
+                    uint64_t* edges) {
+    EG_TRY(check_graph(g, "eg_msbfs_graphs"));
+    return run_msbfs_graphs(g, roots, roots_per_graph, levels, where, edges);
+}
+
+int eg_sssp_graphs(eg_graph* g, const uint32_t* sources, int sources_per_graph, float* dist, int where) {
+    EG_TRY(check_graph(g, "eg_sssp_graphs"));
+    return run_sssp_graphs(g, sources, sources_per_graph, dist, where);
+}
+
+}  // extern "C"
+
+namespace eg {
+int load_edges_impl(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int symmetric, int where,
+                    bool validate) {
     if (edge_bytes != 8 && edge_bytes != 12) {
         set_error("eg_load_edges: edge_bytes must be 8 ({src,dst}) or 12 ({src,dst,float})");
         return EG_ERR_INVALID;
@@ -139,6 +175,8 @@ int eg_load_edges(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int ed
     g->built_csr = g->built_csc = false;
     g->eng.pull_ready = false;
     free_batch_state(g);
+    g->batch_voff.clear();
+    g->batch_eoff.clear();
     g->V = V;
     g->E = total;
     g->E_input = E;
@@ -151,10 +189,13 @@ int eg_load_edges(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int ed
         EG_CUDA(cudaMemcpyAsync(g->edges.ptr, edges, (size_t)E * edge_bytes,
                                 where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, g->stream));
     }
-    EG_TRY(validate_edges(g, E));
+    if (validate) EG_TRY(validate_edges(g, E));
     if (symmetric) EG_TRY(symmetrize_edges(g, E));
     return EG_OK;
 }
+}  // namespace eg
+
+extern "C" {
 
 int eg_build(eg_graph* g, int want_csr, int want_csc) {
     EG_TRY(check_graph(g, "eg_build"));
@@ -396,6 +437,10 @@ int eg_set_option(eg_graph* g, int option, int64_t value) {
         case EG_OPT_DENSE_DIVISOR:
             if (value < 1 || value > (1 << 30)) break;
             g->dense_div = (int)value;
+            return EG_OK;
+        case EG_OPT_CUDA_GRAPH:
+            if (value < 0 || value > 1) break;
+            g->use_cuda_graph = (int)value;
             return EG_OK;
         default:
             set_error("eg_set_option: unknown option %d", option);

@@ -45,6 +45,8 @@ struct MsBfsPullOp {
     uint32_t* n_new;
     unsigned long long* reach_edges;
     const uint32_t* deg;
+    const int* stop;  // captured level loops: set once a level found nothing new
+    __device__ bool stopped() const { return stop && *(volatile const int*)stop; }
     __device__ bool item_active(uint32_t v) const { return __ldcg(visit + v) != full; }
     __device__ Acc identity() const { return 0ull; }
     __device__ Acc gather(uint32_t u, uint64_t) const { return __ldcg(front + u); }
@@ -74,18 +76,6 @@ struct MsBfsPullOp {
         if ((threadIdx.x & 31) == 0 && any) atomicAdd(n_new, (uint32_t)__popc(any));
     }
 };
-
-__global__ void k_msbfs_roots(const uint32_t* roots, int n, unsigned long long* visit, unsigned long long* front,
-                              uint8_t* levels, unsigned long long* reach_edges, const uint32_t* deg) {
-    int s = threadIdx.x;
-    if (s < n) {
-        const uint32_t r = roots[s];
-        atomicOr(visit + r, 1ull << s);
-        atomicOr(front + r, 1ull << s);
-        if (levels) levels[(uint64_t)r * 64 + s] = 0;
-        atomicAdd(reach_edges, (unsigned long long)deg[r]);
-    }
-}
 
 // [V][64] -> [n][V] for the first n columns (32x32 tiles through shared memory)
 __global__ void k_transpose_u8(const uint8_t* __restrict__ in, uint32_t V, int n, uint8_t* __restrict__ out) {
@@ -421,9 +411,18 @@ int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E) {
 // ---------------------------------------------------------------------------------------------
 struct BatchState {
     DevBuf a64, b64, c64, lev, rows0, rows1, heavy, tmp_out, seeds, wn_csc, wn_csr, s_out, gA, row_of, ck, seg;
-    DevBuf ch0, ch1, flag;
+    DevBuf ch0, ch1, flag, level_cnt, entries, n_entries;
     RowTasks csc_tasks, csr_tasks;
     bool csc_ready = false, csr_ready = false;
+    // captured MS-BFS level loop and the shapes it was captured for
+    void* graph_exec = nullptr;
+    uint64_t graph_V = 0;
+    bool graph_lev = false;
+    uint32_t graph_entries = 0;
+    int graph_nbits = 0;
+    ~BatchState() {
+        if (graph_exec) cudaGraphExecDestroy((cudaGraphExec_t)graph_exec);
+    }
 };
 
 static BatchState& bstate(eg_graph* g) {
@@ -459,53 +458,183 @@ static int check_roots(eg_graph* g, const uint32_t* roots, int n, int where, con
     return EG_OK;
 }
 
-int run_msbfs(eg_graph* g, const uint32_t* roots, int n, uint8_t* levels, int where, uint64_t* edges) {
-    if (!g->built_csc) { set_error("eg_msbfs: CSC not built"); return EG_ERR_STATE; }
-    EG_TRY(check_roots(g, roots, n, where, "eg_msbfs"));
-    EG_TRY(ensure_engine(g));
-    EG_TRY(setup_pull(g));
+// root entries (global vertex, bit) from n roots: entry s = (roots[s] + base, s)
+__global__ void k_root_entries(const uint32_t* roots, int n, uint32_t base, uint2* ent) {
+    const int s = threadIdx.x;
+    if (s < n) ent[s] = make_uint2(roots[s] + base, (uint32_t)s);
+}
+
+// per-graph roots of a graph batch: entry (g * nper + s) = (voff[g] + roots[g * nper + s], s)
+__global__ void k_root_entries_graphs(const uint32_t* roots, const uint64_t* voff, uint32_t ngraphs, int nper,
+                                      uint2* ent) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < (uint64_t)ngraphs * nper) {
+        const uint64_t gi = i / nper;
+        ent[i] = make_uint2((uint32_t)(voff[gi] + roots[i]), (uint32_t)(i % nper));
+    }
+}
+
+__global__ void k_msbfs_init_entries(const uint2* ent, const uint32_t* n_dev, unsigned long long* visit,
+                                     unsigned long long* front, uint8_t* levels, unsigned long long* reach_edges,
+                                     const uint32_t* deg) {
+    const uint32_t n = *n_dev;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t v = ent[i].x, s = ent[i].y;
+        const unsigned long long bit = 1ull << s;
+        const unsigned long long old = atomicOr(visit + v, bit);
+        atomicOr(front + v, bit);
+        if (!(old & bit)) {
+            if (levels) levels[(uint64_t)v * 64 + s] = 0;
+            atomicAdd(reach_edges, (unsigned long long)deg[v]);
+        }
+    }
+}
+
+// in a captured level loop: level L runs only if level L-1 found something
+__global__ void k_level_gate(const uint32_t* prev_new, int* stop) {
+    if (*prev_new == 0) *stop = 1;
+}
+
+constexpr int kGraphLevels = 32;
+
+// MS-BFS over root entries already in b.entries (count in b.n_entries device word)
+static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, uint64_t* reach_out, int* sweeps_out) {
     BatchState& b = bstate(g);
     const uint64_t V = g->V;
-    EG_TRY(b.a64.reserve(8 * V + 8));
-    EG_TRY(b.b64.reserve(8 * V + 8));
-    EG_TRY(b.c64.reserve(8 * V + 8));
-    if (levels) EG_TRY(b.lev.reserve(64 * V + 64));
-    EG_TRY(copy_small_in(g, b.seeds, roots, n, where));
     unsigned long long* visit = b.a64.as<unsigned long long>();
-    unsigned long long* front = b.b64.as<unsigned long long>();
-    unsigned long long* next = b.c64.as<unsigned long long>();
-    uint8_t* lev = levels ? b.lev.as<uint8_t>() : nullptr;
-    uint32_t* d_new = reinterpret_cast<uint32_t*>(g->eng.counters.as<unsigned long long>() + 2);
+    unsigned long long* bufA = b.b64.as<unsigned long long>();
+    unsigned long long* bufB = b.c64.as<unsigned long long>();
+    uint32_t* cnt = b.level_cnt.as<uint32_t>();  // [kGraphLevels + 1]
+    int* stop = reinterpret_cast<int*>(cnt + kGraphLevels + 1);
     unsigned long long* d_reach = g->eng.counters.as<unsigned long long>() + 4;
-    {
-        Timed t(&g->prof, g->stream, "msbfs_init");
+    const unsigned long long full = nbits == 64 ? ~0ull : ((1ull << nbits) - 1ull);
+    const uint32_t* deg = g->outdeg.as<uint32_t>();
+    const unsigned init_grid = std::max(1u, std::min<unsigned>((n_entries + 255) / 256, 4096u));
+
+    auto enqueue_init = [&]() -> int {
         EG_CUDA(cudaMemsetAsync(visit, 0, 8 * V, g->stream));
-        EG_CUDA(cudaMemsetAsync(front, 0, 8 * V, g->stream));
+        EG_CUDA(cudaMemsetAsync(bufA, 0, 8 * V, g->stream));
         EG_CUDA(cudaMemsetAsync(d_reach, 0, 8, g->stream));
+        EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (kGraphLevels + 2), g->stream));
         if (lev) EG_CUDA(cudaMemsetAsync(lev, 0xFF, 64 * V, g->stream));
-        k_msbfs_roots<<<1, 64, 0, g->stream>>>(b.seeds.as<uint32_t>(), n, visit, front, lev, d_reach, g->outdeg.as<uint32_t>());
-        EG_CHECK_LAUNCH("k_msbfs_roots");
-    }
-    const unsigned long long full = n == 64 ? ~0ull : ((1ull << n) - 1ull);
-    uint32_t lvl = 0;
+        k_msbfs_init_entries<<<init_grid, 256, 0, g->stream>>>(b.entries.as<uint2>(), b.n_entries.as<uint32_t>(), visit,
+                                                               bufA, lev, d_reach, deg);
+        EG_CHECK_LAUNCH("k_msbfs_init_entries");
+        return EG_OK;
+    };
+    auto enqueue_level = [&](uint32_t lvl, uint32_t* counter, const int* stop_flag) -> int {
+        unsigned long long* front = (lvl & 1) ? bufB : bufA;
+        unsigned long long* next = (lvl & 1) ? bufA : bufB;
+        EG_CUDA(cudaMemsetAsync(next, 0, 8 * V, g->stream));
+        MsBfsPullOp op{front, visit, next, lev, lvl + 1, full, counter, d_reach, deg, stop_flag};
+        return launch_pull(g, op, "msbfs_pull");
+    };
+
     int sweeps = 0;
+    uint32_t lvl = 0;
+    if (g->use_cuda_graph) {
+        // init + kGraphLevels levels replayed as one CUDA graph; levels after an empty one stop at
+        // their first instruction (k_level_gate sets the flag the pull kernel checks)
+        const bool key_ok = b.graph_exec && b.graph_V == V && b.graph_lev == (lev != nullptr) &&
+                            b.graph_entries >= n_entries && b.graph_nbits == nbits;
+        if (!key_ok) {
+            if (b.graph_exec) cudaGraphExecDestroy((cudaGraphExec_t)b.graph_exec);
+            b.graph_exec = nullptr;
+            const bool prof = g->prof.enabled;
+            g->prof.enabled = false;
+            EG_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+            int st = enqueue_init();
+            for (uint32_t L = 0; st == EG_OK && L < (uint32_t)kGraphLevels; ++L) {
+                if (L > 0) {
+                    k_level_gate<<<1, 1, 0, g->stream>>>(cnt + L - 1, stop);
+                    st = cudaGetLastError() == cudaSuccess ? EG_OK : EG_ERR_CUDA;
+                }
+                if (st == EG_OK) st = enqueue_level(L, cnt + L, stop);
+            }
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(g->stream, &graph);
+            g->prof.enabled = prof;
+            EG_TRY(st);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+            cudaGraphExec_t exec = nullptr;
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+            b.graph_exec = exec;
+            b.graph_V = V;
+            b.graph_lev = lev != nullptr;
+            b.graph_entries = n_entries;
+            b.graph_nbits = nbits;
+        }
+        {
+            Timed t(&g->prof, g->stream, "msbfs_graph");
+            EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)b.graph_exec, g->stream));
+        }
+        std::vector<uint32_t> h(kGraphLevels);
+        EG_CUDA(cudaMemcpyAsync(h.data(), cnt, sizeof(uint32_t) * kGraphLevels, cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaStreamSynchronize(g->stream));
+        for (int L = 0; L < kGraphLevels; ++L) {
+            ++sweeps;
+            if (h[L] == 0) break;
+        }
+        if (h[kGraphLevels - 1] == 0) {
+            if (reach_out) EG_CUDA(cudaMemcpy(reach_out, d_reach, 8, cudaMemcpyDeviceToHost));
+            *sweeps_out = sweeps;
+            return EG_OK;
+        }
+        lvl = kGraphLevels;  // deeper than the captured levels: continue below
+    } else {
+        EG_TRY(enqueue_init());
+    }
+    uint32_t* d_new = cnt + kGraphLevels;
     while (true) {
         if (lvl >= 254) {
             set_error("eg_msbfs: more than 254 levels");
             return EG_ERR_UNSUPPORTED;
         }
-        EG_CUDA(cudaMemsetAsync(next, 0, 8 * V, g->stream));
         EG_CUDA(cudaMemsetAsync(d_new, 0, 4, g->stream));
-        MsBfsPullOp op{front, visit, next, lev, lvl + 1, full, d_new, d_reach, g->outdeg.as<uint32_t>()};
-        EG_TRY(launch_pull(g, op, "msbfs_pull"));
+        EG_TRY(enqueue_level(lvl, d_new, nullptr));
         ++sweeps;
         uint32_t h = 0;
         EG_CUDA(cudaMemcpyAsync(&h, d_new, 4, cudaMemcpyDeviceToHost, g->stream));
         EG_CUDA(cudaStreamSynchronize(g->stream));
         if (!h) break;
-        std::swap(front, next);
         ++lvl;
     }
+    if (reach_out) EG_CUDA(cudaMemcpy(reach_out, d_reach, 8, cudaMemcpyDeviceToHost));
+    *sweeps_out = sweeps;
+    return EG_OK;
+}
+
+static int msbfs_buffers(eg_graph* g, uint32_t n_entries, bool with_levels) {
+    BatchState& b = bstate(g);
+    const uint64_t V = g->V;
+    EG_TRY(ensure_engine(g));
+    EG_TRY(setup_pull(g));
+    EG_TRY(b.a64.reserve(8 * V + 8));
+    EG_TRY(b.b64.reserve(8 * V + 8));
+    EG_TRY(b.c64.reserve(8 * V + 8));
+    EG_TRY(b.level_cnt.reserve(sizeof(uint32_t) * (kGraphLevels + 4)));
+    EG_TRY(b.entries.reserve(sizeof(uint2) * (n_entries + 1)));
+    EG_TRY(b.n_entries.reserve(16));
+    if (with_levels) EG_TRY(b.lev.reserve(64 * V + 64));
+    EG_CUDA(cudaMemcpyAsync(b.n_entries.ptr, &n_entries, 4, cudaMemcpyHostToDevice, g->stream));
+    return EG_OK;
+}
+
+int run_msbfs(eg_graph* g, const uint32_t* roots, int n, uint8_t* levels, int where, uint64_t* edges) {
+    if (!g->built_csc) { set_error("eg_msbfs: CSC not built"); return EG_ERR_STATE; }
+    EG_TRY(check_roots(g, roots, n, where, "eg_msbfs"));
+    BatchState& b = bstate(g);
+    const uint64_t V = g->V;
+    EG_TRY(msbfs_buffers(g, (uint32_t)n, levels != nullptr));
+    EG_TRY(copy_small_in(g, b.seeds, roots, n, where));
+    k_root_entries<<<1, 64, 0, g->stream>>>(b.seeds.as<uint32_t>(), n, 0, b.entries.as<uint2>());
+    EG_CHECK_LAUNCH("k_root_entries");
+    uint8_t* lev = levels ? b.lev.as<uint8_t>() : nullptr;
+    uint64_t reach = 0;
+    int sweeps = 0;
+    EG_TRY(msbfs_core(g, (uint32_t)n, n, lev, &reach, &sweeps));
     if (levels) {
         uint8_t* out = levels;
         if (where != EG_DEVICE) {
@@ -518,8 +647,6 @@ int run_msbfs(eg_graph* g, const uint32_t* roots, int n, uint8_t* levels, int wh
         if (where != EG_DEVICE)
             EG_CUDA(cudaMemcpyAsync(levels, out, (size_t)n * V, cudaMemcpyDeviceToHost, g->stream));
     }
-    unsigned long long reach = 0;
-    EG_CUDA(cudaMemcpyAsync(&reach, d_reach, 8, cudaMemcpyDeviceToHost, g->stream));
     EG_CUDA(cudaStreamSynchronize(g->stream));
     if (edges) *edges = reach;
     g->last_edges_processed = reach;
@@ -639,6 +766,7 @@ static int ppr_common(eg_graph* g, const float* w_in, const uint32_t* seeds, int
 struct PprPullOp {
     using Acc = float;
     static constexpr bool kFilter = false;
+    __device__ bool stopped() const { return false; }
     __device__ bool item_active(uint32_t) const { return true; }
     const float* x;
     const float* wn;
@@ -833,14 +961,18 @@ int run_ppr_backward(eg_graph* g, const float* w_in, const uint32_t* seeds, int 
 }
 
 // ---------------------------------------------------------------------------------------------
-int run_sssp_batch(eg_graph* g, const uint32_t* srcs, int n, float* out, int where) {
-    if (!g->built_csc) { set_error("eg_sssp_batch: CSC not built"); return EG_ERR_STATE; }
-    if (!g->weighted || g->edge_ids) { set_error("eg_sssp_batch: graph needs float edge weights"); return EG_ERR_STATE; }
-    EG_TRY(check_roots(g, srcs, n, where, "eg_sssp_batch"));
+__global__ void k_sssp_init_entries(const uint2* ent, uint32_t n, float* dist, uint8_t* changed) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        dist[(uint64_t)ent[i].x * 64 + ent[i].y] = 0.f;
+        changed[ent[i].x] = 1;
+    }
+}
+
+// Bellman-Ford sweeps from the root entries in b.entries; leaves dist [V][64] in b.rows0
+static int sssp_core(eg_graph* g, uint32_t n_entries, int* sweeps_out) {
     EG_TRY(ensure_tasks(g, false));
     BatchState& b = bstate(g);
     const uint64_t V = g->V;
-    EG_TRY(copy_small_in(g, b.seeds, srcs, n, where));
     EG_TRY(b.rows0.reserve(256 * V + 256));
     EG_TRY(b.ch0.reserve(V + 64));
     EG_TRY(b.ch1.reserve(V + 64));
@@ -851,8 +983,9 @@ int run_sssp_batch(eg_graph* g, const uint32_t* srcs, int n, float* out, int whe
         k_fill_f32_rows<<<grid_for(64 * V, 256, 152u * 16u), 256, 0, g->stream>>>(dist, 64 * V, 1e9f);
         EG_CHECK_LAUNCH("k_fill_f32_rows");
         EG_CUDA(cudaMemsetAsync(b.ch0.ptr, 0, V, g->stream));
-        k_sssp_batch_init<<<1, 64, 0, g->stream>>>(b.seeds.as<uint32_t>(), n, dist, b.ch0.as<uint8_t>());
-        EG_CHECK_LAUNCH("k_sssp_batch_init");
+        k_sssp_init_entries<<<std::max(1u, std::min<unsigned>((n_entries + 255) / 256, 4096u)), 256, 0, g->stream>>>(
+            b.entries.as<uint2>(), n_entries, dist, b.ch0.as<uint8_t>());
+        EG_CHECK_LAUNCH("k_sssp_init_entries");
     }
     RowArgs a = row_args(b.csc_tasks, g->cvert.as<uint32_t>(), g->csc_adj.as<uint32_t>(), g->csc_w.as<float>());
     uint8_t* prev = b.ch0.as<uint8_t>();
@@ -873,6 +1006,27 @@ int run_sssp_batch(eg_graph* g, const uint32_t* srcs, int n, float* out, int whe
         if (!any) break;
         std::swap(prev, nxt);
     }
+    *sweeps_out = sweeps;
+    return EG_OK;
+}
+
+static int sssp_ready(eg_graph* g, const char* fn) {
+    if (!g->built_csc) { set_error("%s: CSC not built", fn); return EG_ERR_STATE; }
+    if (!g->weighted || g->edge_ids) { set_error("%s: graph needs float edge weights", fn); return EG_ERR_STATE; }
+    return EG_OK;
+}
+
+int run_sssp_batch(eg_graph* g, const uint32_t* srcs, int n, float* out, int where) {
+    EG_TRY(sssp_ready(g, "eg_sssp_batch"));
+    EG_TRY(check_roots(g, srcs, n, where, "eg_sssp_batch"));
+    BatchState& b = bstate(g);
+    const uint64_t V = g->V;
+    EG_TRY(copy_small_in(g, b.seeds, srcs, n, where));
+    EG_TRY(b.entries.reserve(sizeof(uint2) * 64));
+    k_root_entries<<<1, 64, 0, g->stream>>>(b.seeds.as<uint32_t>(), n, 0, b.entries.as<uint2>());
+    EG_CHECK_LAUNCH("k_root_entries");
+    int sweeps = 0;
+    EG_TRY(sssp_core(g, (uint32_t)n, &sweeps));
     if (out) {
         float* dst = out;
         if (where != EG_DEVICE) {
@@ -880,7 +1034,7 @@ int run_sssp_batch(eg_graph* g, const uint32_t* srcs, int n, float* out, int whe
             dst = b.tmp_out.as<float>();
         }
         dim3 blk(32, 8);
-        k_transpose_rows<float><<<(unsigned)((V + 31) / 32), blk, 0, g->stream>>>(dist, (uint32_t)V, n, dst);
+        k_transpose_rows<float><<<(unsigned)((V + 31) / 32), blk, 0, g->stream>>>(b.rows0.as<float>(), (uint32_t)V, n, dst);
         EG_CHECK_LAUNCH("k_transpose_rows");
         if (where != EG_DEVICE) EG_CUDA(cudaMemcpyAsync(out, dst, 4ull * n * V, cudaMemcpyDeviceToHost, g->stream));
     }
@@ -889,6 +1043,137 @@ int run_sssp_batch(eg_graph* g, const uint32_t* srcs, int n, float* out, int whe
     g->last_pulls = sweeps;
     g->last_pushes = 0;
     return EG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// many small graphs: roots are local ids, nper per graph; outputs stay vertex-major [V_total][64]
+static int graph_roots(eg_graph* g, const uint32_t* roots, int nper, int where, const char* fn, uint32_t* n_entries) {
+    const uint64_t G = g->batch_voff.size() ? g->batch_voff.size() - 1 : 0;
+    if (!G) { set_error("%s: no graph batch loaded (eg_load_graph_batch)", fn); return EG_ERR_STATE; }
+    if (!roots || nper < 1 || nper > 64) { set_error("%s: need 1..64 roots per graph", fn); return EG_ERR_INVALID; }
+    const uint64_t n = G * (uint64_t)nper;
+    std::vector<uint32_t> h(n);
+    EG_CUDA(cudaMemcpy(h.data(), roots, 4 * n, where == EG_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint64_t gi = i / nper;
+        if (h[i] >= g->batch_voff[gi + 1] - g->batch_voff[gi]) {
+            set_error("%s: root %u of graph %llu out of range", fn, h[i], (unsigned long long)gi);
+            return EG_ERR_INVALID;
+        }
+    }
+    BatchState& b = bstate(g);
+    EG_TRY(b.entries.reserve(sizeof(uint2) * (n + 1)));
+    EG_TRY(b.tmp_out.reserve(4 * n + 64));
+    EG_CUDA(cudaMemcpyAsync(b.tmp_out.ptr, h.data(), 4 * n, cudaMemcpyHostToDevice, g->stream));
+    k_root_entries_graphs<<<(unsigned)((n + 255) / 256), 256, 0, g->stream>>>(
+        b.tmp_out.as<uint32_t>(), g->d_batch_voff.as<uint64_t>(), (uint32_t)G, nper, b.entries.as<uint2>());
+    EG_CHECK_LAUNCH("k_root_entries_graphs");
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    *n_entries = (uint32_t)n;
+    return EG_OK;
+}
+
+int run_msbfs_graphs(eg_graph* g, const uint32_t* roots, int nper, uint8_t* levels, int where, uint64_t* edges) {
+    if (!g->built_csc) { set_error("eg_msbfs_graphs: CSC not built"); return EG_ERR_STATE; }
+    uint32_t n = 0;
+    const uint64_t G = g->batch_voff.size() ? g->batch_voff.size() - 1 : 0;
+    EG_TRY(msbfs_buffers(g, (uint32_t)(G * (uint64_t)std::max(nper, 1)), levels != nullptr));
+    EG_TRY(graph_roots(g, roots, nper, where, "eg_msbfs_graphs", &n));
+    BatchState& b = bstate(g);
+    EG_CUDA(cudaMemcpyAsync(b.n_entries.ptr, &n, 4, cudaMemcpyHostToDevice, g->stream));
+    uint64_t reach = 0;
+    int sweeps = 0;
+    EG_TRY(msbfs_core(g, n, nper, levels ? b.lev.as<uint8_t>() : nullptr, &reach, &sweeps));
+    if (levels)
+        EG_CUDA(cudaMemcpyAsync(levels, b.lev.ptr, 64ull * g->V,
+                                where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    if (edges) *edges = reach;
+    g->last_edges_processed = reach;
+    g->last_iterations = sweeps;
+    g->last_pulls = sweeps;
+    g->last_pushes = 0;
+    return EG_OK;
+}
+
+int run_sssp_graphs(eg_graph* g, const uint32_t* sources, int nper, float* dist, int where) {
+    EG_TRY(sssp_ready(g, "eg_sssp_graphs"));
+    uint32_t n = 0;
+    EG_TRY(graph_roots(g, sources, nper, where, "eg_sssp_graphs", &n));
+    int sweeps = 0;
+    EG_TRY(sssp_core(g, n, &sweeps));
+    if (dist)
+        EG_CUDA(cudaMemcpyAsync(dist, bstate(g).rows0.ptr, 256ull * g->V,
+                                where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    g->last_iterations = sweeps;
+    g->last_pulls = sweeps;
+    g->last_pushes = 0;
+    return EG_OK;
+}
+
+// graph i's edges occupy [eoff[i], eoff[i+1]); its vertex v becomes voff[i] + v
+__global__ void k_relabel_batch(uint8_t* edges, int rec, uint64_t E, const uint64_t* __restrict__ eoff,
+                                const uint64_t* __restrict__ voff, uint32_t G, int* bad) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < E; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = G;  // last graph with eoff <= i
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(eoff + mid) <= i) lo = mid; else hi = mid;
+        }
+        uint32_t* r = reinterpret_cast<uint32_t*>(edges + i * (uint64_t)rec);
+        const uint64_t base = voff[lo], nv = voff[lo + 1] - base;
+        if (r[0] >= nv || r[1] >= nv) {
+            atomicExch(bad, 1);
+            continue;
+        }
+        r[0] = (uint32_t)(base + r[0]);
+        r[1] = (uint32_t)(base + r[1]);
+    }
+}
+
+int load_graph_batch(eg_graph* g, const void* edges, int rec, const uint64_t* eoff, const uint32_t* nverts, int G,
+                     int where) {
+    if ((rec != 8 && rec != 12) || G < 1 || !eoff || !nverts || eoff[0] != 0 || (where != EG_HOST && where != EG_DEVICE)) {
+        set_error("eg_load_graph_batch: need 8/12-byte records, G >= 1, edge offsets starting at 0, vertex counts");
+        return EG_ERR_INVALID;
+    }
+    std::vector<uint64_t> voff(G + 1, 0), eo(eoff, eoff + G + 1);
+    for (int i = 0; i < G; ++i) {
+        if (nverts[i] == 0 || eo[i + 1] < eo[i]) {
+            set_error("eg_load_graph_batch: graph %d has no vertices or negative edge count", i);
+            return EG_ERR_INVALID;
+        }
+        voff[i + 1] = voff[i] + nverts[i];
+    }
+    if (voff[G] >= (1ull << 32)) {
+        set_error("eg_load_graph_batch: more than 2^32 vertices in total");
+        return EG_ERR_INVALID;
+    }
+    const uint64_t E = eo[G];
+    EG_TRY(load_edges_impl(g, edges, E, (uint32_t)voff[G], rec, 0, where, false));
+    EG_TRY(g->d_batch_voff.reserve(8 * (G + 1)));
+    EG_TRY(g->tmp64.reserve(8 * (G + 1)));
+    EG_CUDA(cudaMemcpyAsync(g->d_batch_voff.ptr, voff.data(), 8 * (G + 1), cudaMemcpyHostToDevice, g->stream));
+    EG_CUDA(cudaMemcpyAsync(g->tmp64.ptr, eo.data(), 8 * (G + 1), cudaMemcpyHostToDevice, g->stream));
+    EG_CUDA(cudaMemsetAsync(g->err.as<int>() + 1, 0, sizeof(int), g->stream));
+    if (E) {
+        Timed t(&g->prof, g->stream, "relabel_batch");
+        k_relabel_batch<<<grid_for(E, 256, 152u * 16u), 256, 0, g->stream>>>(
+            g->edges.as<uint8_t>(), rec, E, g->tmp64.as<uint64_t>(), g->d_batch_voff.as<uint64_t>(), (uint32_t)G,
+            g->err.as<int>() + 1);
+        EG_CHECK_LAUNCH("k_relabel_batch");
+    }
+    int bad = 0;
+    EG_CUDA(cudaMemcpyAsync(&bad, g->err.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    if (bad) {
+        set_error("eg_load_graph_batch: a record holds a vertex id >= its graph's vertex count");
+        return EG_ERR_INVALID;
+    }
+    g->batch_voff = voff;
+    g->batch_eoff = eo;
+    return build_structures(g, 1, 1);
 }
 
 }  // namespace eg

@@ -173,6 +173,10 @@ struct eg_graph {
     // engine options (eg_set_option)
     int bfs_direction = 0;  // 0: Gemini threshold switch, 1: push only, 2: pull only
     int dense_div = 20;     // sparse iff active_edges < E / dense_div (core/graph.hpp:1491)
+    int use_cuda_graph = 0; // batched BFS: replay the level loop as one captured CUDA graph
+    // many small graphs in one handle (eg_load_graph_batch): per-graph vertex / edge offsets
+    std::vector<uint64_t> batch_voff, batch_eoff;
+    eg::DevBuf d_batch_voff;
     // last operator statistics
     uint64_t last_edges_processed = 0;
     int last_iterations = 0;
@@ -203,6 +207,12 @@ int run_ppr_backward(eg_graph* g, const float* w_in, const uint32_t* seeds, int 
                      const float* dl_dx, float* dl_dw, int where);
 int run_sssp_batch(eg_graph* g, const uint32_t* srcs, int n, float* out, int where);
 void free_batch_state(eg_graph* g);
+int load_edges_impl(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int symmetric, int where,
+                    bool validate);
+int load_graph_batch(eg_graph* g, const void* edges, int rec, const uint64_t* eoff, const uint32_t* nverts, int G,
+                     int where);
+int run_msbfs_graphs(eg_graph* g, const uint32_t* roots, int nper, uint8_t* levels, int where, uint64_t* edges);
+int run_sssp_graphs(eg_graph* g, const uint32_t* sources, int nper, float* dist, int where);
 int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E);
 
 // device helpers

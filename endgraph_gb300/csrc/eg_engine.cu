@@ -44,6 +44,7 @@ struct BfsOp {  // toolkits/bfs.cpp:52-58: first visitor of dst becomes its pare
 struct BfsPullOp {
     using Acc = uint32_t;
     static constexpr bool kFilter = true;
+    __device__ bool stopped() const { return false; }
     const unsigned long long* front;
     unsigned long long* visited;
     unsigned long long* next_front;
@@ -109,6 +110,7 @@ struct CcPushOp {  // toolkits/cc.cpp:50-60: msg = label[src]; write_min(label[d
 struct PrPullOp {  // toolkits/pagerank.cpp:64-97: sum curr[src]; next = 1-d+d*sum (/ outdeg)
     using Acc = float;
     static constexpr bool kFilter = false;
+    __device__ bool stopped() const { return false; }
     __device__ bool item_active(uint32_t) const { return true; }
     const float* curr;
     float* next;
@@ -138,6 +140,7 @@ struct PrPullOp {  // toolkits/pagerank.cpp:64-97: sum curr[src]; next = 1-d+d*s
 struct CcPullOp {  // toolkits/cc.cpp:62-80: min label over in-neighbours, write_min + activate
     using Acc = uint32_t;
     static constexpr bool kFilter = false;
+    __device__ bool stopped() const { return false; }
     __device__ bool item_active(uint32_t) const { return true; }
     uint32_t* label;
     unsigned long long* next_bm;

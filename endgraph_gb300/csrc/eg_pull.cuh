@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
                                                         const uint32_t* __restrict__ chunk_item, uint64_t E,
                                                         uint64_t nitems, uint64_t nchunks, uint32_t V, int cap) {
     using Acc = typename Op::Acc;
+    if (op.stopped()) return;  // a captured loop whose traversal already finished
     extern __shared__ __align__(16) unsigned char s_raw[];
     // item boundaries relative to the chunk start, clamped to [0, chunk]: 4 bytes per item
     uint32_t* s_idx = reinterpret_cast<uint32_t*>(s_raw);

@@ -167,8 +167,10 @@ int eg_sssp(eg_graph* g, uint32_t root, float* dist, int where);
  * vertices' out-edges < E / divisor (core/graph.hpp:1484-1491; the reference uses 20).
  * EG_OPT_BFS_DIRECTION: 0 applies that switch to BFS with the toolkit's dense callbacks
  * (toolkits/bfs.cpp:60-76), 1 forces push every level as the reference's use_root flag does
- * (core/graph.hpp:1496-1498), 2 forces pull.  Results are identical in every mode. */
-enum { EG_OPT_BFS_DIRECTION = 1, EG_OPT_DENSE_DIVISOR = 2 };
+ * (core/graph.hpp:1496-1498), 2 forces pull.  Results are identical in every mode.
+ * EG_OPT_CUDA_GRAPH: 1 replays the batched-BFS level loop (eg_msbfs, eg_msbfs_graphs) as one
+ * captured CUDA graph of 32 levels instead of one host round trip per level. */
+enum { EG_OPT_BFS_DIRECTION = 1, EG_OPT_DENSE_DIVISOR = 2, EG_OPT_CUDA_GRAPH = 3 };
 int eg_set_option(eg_graph* g, int option, int64_t value);
 
 /* ---- batched operators (no reference counterpart: batched forms of the toolkits) ---------- */
@@ -192,6 +194,22 @@ int eg_ppr(eg_graph* g, const float* weights, const uint32_t* seeds, int nseeds,
  * stored every ceil(sqrt(iterations)) steps. */
 int eg_ppr_backward(eg_graph* g, const float* weights, const uint32_t* seeds, int nseeds, float alpha, int iterations,
                     const float* dl_dx, float* dl_dw, int where);
+
+/* Many independent graphs in one handle: graph i's records are edges[graph_edges[i] ..
+ * graph_edges[i+1]) with local ids < graph_vertices[i]; the handle holds their disjoint union (graph
+ * i's vertex v is union vertex voff[i] + v) and preprocesses all of them with one build (one launch
+ * per build pass for the whole batch).  graph_edges[G+1] and graph_vertices[G] are host arrays. */
+int eg_load_graph_batch(eg_graph* g, const void* edges, int edge_bytes, const uint64_t* graph_edges,
+                        const uint32_t* graph_vertices, int ngraphs, int where);
+/* voff[G+1] and the edge offsets [G+1] of the loaded batch (host arrays; either may be NULL) */
+int eg_get_graph_batch(eg_graph* g, uint64_t* vertex_offsets, uint64_t* edge_offsets);
+/* Bit-parallel BFS with roots_per_graph <= 64 roots in every graph of the batch (roots[G * n],
+ * local ids): levels[V_total][64] bytes, row = union vertex, column = root index, 0xFF unreached. */
+int eg_msbfs_graphs(eg_graph* g, const uint32_t* roots, int roots_per_graph, uint8_t* levels, int where,
+                    uint64_t* edges);
+/* Bellman-Ford with sources_per_graph <= 64 sources in every graph (weighted batch):
+ * dist[V_total][64] floats, row = union vertex, column = source index, 1e9 unreachable. */
+int eg_sssp_graphs(eg_graph* g, const uint32_t* sources, int sources_per_graph, float* dist, int where);
 
 /* statistics of the last toolkit call: edges traversed, iterations, push / pull iterations */
 int eg_last_run(eg_graph* g, uint64_t* edges_processed, int* iterations, int* push_iters, int* pull_iters);

@@ -30,6 +30,85 @@ def test_msbfs_matches_single_source(eg_lib):
         assert edges == total
 
 
+@pytest.mark.parametrize("cuda_graph", [0, 1])
+def test_msbfs_cuda_graph_mode(eg_lib, cuda_graph):
+    """The captured 32-level loop gives the same levels as the host-driven loop."""
+    import endgraph_gb300 as eg
+    V, E = 1 << 13, 1 << 16
+    src, dst, _ = rmat_graph(V, E, 97)
+    csr = oracle.build_csr(src, dst, None, V, np.array([0, V], np.uint32))
+    roots = np.array(src[:64], np.uint32)
+    with eg.Graph() as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        g.set_option(eg.EG_OPT_CUDA_GRAPH, cuda_graph)
+        for rep in range(2):  # the second call replays the cached graph
+            levels, _ = g.msbfs(roots[rep * 8:] if rep else roots)
+            use = roots[rep * 8:] if rep else roots
+            for s in (0, 5, len(use) - 1):
+                ref = oracle.bfs_levels(csr["off"][0], csr["adj"], V, int(use[s]))
+                assert np.array_equal(levels[s], np.where(ref == oracle.UNREACHED, 255, ref).astype(np.uint8))
+
+
+def _graph_batch(G, seed, weighted=False):
+    rng = np.random.default_rng(seed)
+    Vs = np.exp(rng.uniform(np.log(100), np.log(5000), G)).astype(np.uint32)
+    efs = rng.integers(4, 33, G)
+    parts = []
+    for i in range(G):
+        s, d, w = rmat_graph(int(Vs[i]), int(Vs[i] * efs[i]), seed * 1000 + i, weights=(0.0, 1.0) if weighted else None)
+        parts.append((s, d, w))
+    eoff = np.zeros(G + 1, np.uint64)
+    eoff[1:] = np.cumsum([len(p[0]) for p in parts])
+    src = np.concatenate([p[0] for p in parts])
+    dst = np.concatenate([p[1] for p in parts])
+    w = np.concatenate([p[2] for p in parts]) if weighted else None
+    return Vs, eoff, parts, src, dst, w
+
+
+@pytest.mark.parametrize("cuda_graph", [0, 1])
+def test_graph_batch_msbfs(eg_lib, cuda_graph):
+    """Many small graphs preprocessed together; 64 roots per graph; every graph matches the oracle."""
+    import endgraph_gb300 as eg
+    G = 40
+    Vs, eoff, parts, src, dst, _ = _graph_batch(G, 7)
+    rng = np.random.default_rng(1)
+    roots = np.concatenate([rng.integers(0, Vs[i], 64) for i in range(G)]).astype(np.uint32)
+    with eg.Graph() as g:
+        g.load_graph_batch(eg.pack_edges(src, dst), eoff, Vs)
+        g.set_option(eg.EG_OPT_CUDA_GRAPH, cuda_graph)
+        voff, eo = g.graph_batch()
+        assert np.array_equal(eo, eoff) and voff[-1] == Vs.sum()
+        levels, _ = g.msbfs_graphs(roots, 64)
+    for i in (0, 1, G // 2, G - 1):
+        s, d, _ = parts[i]
+        V = int(Vs[i])
+        csr = oracle.build_csr(s, d, None, V, np.array([0, V], np.uint32))
+        block = levels[voff[i]:voff[i + 1]]
+        for j in (0, 17, 63):
+            ref = oracle.bfs_levels(csr["off"][0], csr["adj"], V, int(roots[i * 64 + j]))
+            assert np.array_equal(block[:, j], np.where(ref == oracle.UNREACHED, 255, ref).astype(np.uint8)), (i, j)
+
+
+def test_graph_batch_sssp(eg_lib):
+    import endgraph_gb300 as eg
+    G = 24
+    Vs, eoff, parts, src, dst, w = _graph_batch(G, 8, weighted=True)
+    rng = np.random.default_rng(2)
+    sources = np.concatenate([rng.integers(0, Vs[i], 64) for i in range(G)]).astype(np.uint32)
+    with eg.Graph() as g:
+        g.load_graph_batch(eg.pack_edges(src, dst, w), eoff, Vs)
+        voff, _ = g.graph_batch()
+        dist = g.sssp_graphs(sources, 64)
+    for i in (0, G // 3, G - 1):
+        s, d, ww = parts[i]
+        V = int(Vs[i])
+        csr = oracle.build_csr(s, d, ww, V, np.array([0, V], np.uint32))
+        for j in (0, 31, 63):
+            ref = oracle.sssp(csr["off"][0], csr["adj"], csr["w"], V, int(sources[i * 64 + j]))
+            got = dist[voff[i]:voff[i + 1], j]
+            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (i, j)
+
+
 def test_sssp_batch_matches_single_source(eg_lib):
     import endgraph_gb300 as eg
     V, E = 1 << 13, 1 << 17
