@@ -47,6 +47,7 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--ppr-scale", type=int, default=22)
+    p.add_argument("--batch-graphs", type=int, default=1024)
     return p.parse_args()
 
 
@@ -271,6 +272,53 @@ def run_batched(args, g, edges, roots, dev, stream):
     return res
 
 
+def run_graph_batch(args, dev):
+    """1,024 independent R-MAT graphs (V log-uniform in [1e3, 5e5], edge factor uniform in 4..32,
+    U[0,1) float weights): one batched build, autotuning, 64 BFS roots and 64 SSSP sources per graph."""
+    import numpy as np
+    import torch
+
+    import endgraph_gb300 as eg
+    G = args.batch_graphs
+    rng = np.random.default_rng(args.seed + 11)
+    Vs = np.exp(rng.uniform(np.log(1e3), np.log(5e5), G)).astype(np.uint32)
+    efs = rng.integers(4, 33, G)
+    Es = Vs.astype(np.uint64) * efs.astype(np.uint64)
+    eoff = np.zeros(G + 1, np.uint64)
+    eoff[1:] = np.cumsum(Es)
+    E = int(eoff[-1])
+    rec = torch.empty((E, 3), dtype=torch.int32, device=dev)
+    for i in range(G):
+        eg.generate_rmat(rec[int(eoff[i]):int(eoff[i + 1])], int(Vs[i]), int(Es[i]), args.seed + 1000 + i, 0.57, 0.19,
+                         0.19, permute=True, weights=(0.0, 1.0))
+    roots = np.concatenate([rng.integers(0, Vs[i], 64) for i in range(G)]).astype(np.uint32)
+    out = {"graphs": G, "V_total": int(Vs.sum()), "E_total": E}
+    with eg.Graph(eta=1, device=dev.index or 0) as g:
+        s = torch.cuda.ExternalStream(g.stream, device=dev)
+        g.load_graph_batch(rec, eoff, Vs)  # warm (allocations)
+        t_b, _ = _timed(s, lambda: g.load_graph_batch(rec, eoff, Vs))  # records -> union -> CPBT + CSR + CSC
+        del rec
+        torch.cuda.empty_cache()
+        out["build_ms"] = round(t_b, 3)
+        out["build_medges_s"] = round(E / t_b / 1e3, 1)
+        tune = g.autotune(roots[:64])  # graph 0's roots are union ids too (its offset is 0)
+        out["autotune"] = tune
+        lev = torch.empty((int(Vs.sum()), 64), dtype=torch.uint8, device=dev)
+        for cg in (0, 1):
+            g.set_option(eg.EG_OPT_CUDA_GRAPH, cg)
+            g.msbfs_graphs(roots, 64, lev)
+            t, (_, edges) = _timed(s, lambda: g.msbfs_graphs(roots, 64, lev))
+            out[f"msbfs_{'graph' if cg else 'host'}_ms"] = round(t, 3)
+            out[f"msbfs_{'graph' if cg else 'host'}_gteps"] = round(edges / t / 1e6, 1)
+        g.set_option(eg.EG_OPT_CUDA_GRAPH, tune["cuda_graph"])
+        del lev
+        dist = torch.empty((int(Vs.sum()), 64), dtype=torch.float32, device=dev)
+        t, _ = _timed(s, lambda: g.sssp_graphs(roots, 64, dist))
+        out["sssp64_ms"] = round(t, 3)
+        out["sssp64_sweeps"] = g.last_run()["iterations"]
+    return out
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -397,6 +445,11 @@ def run_ours(args, world, rank, local):
         del host
 
     batched = None if args.no_batched else run_batched(args, g, edges, roots_all, dev, stream)
+    if batched is not None and args.batch_graphs > 0:
+        g.close()
+        del edges
+        torch.cuda.empty_cache()
+        batched["graph_batch"] = run_graph_batch(args, dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

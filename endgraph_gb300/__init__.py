@@ -22,6 +22,7 @@ LIB_PATH = _build.LIB
 
 EG_HOST, EG_DEVICE = 0, 1
 EG_OPT_BFS_DIRECTION, EG_OPT_DENSE_DIVISOR, EG_OPT_CUDA_GRAPH = 1, 2, 3
+EG_OPT_PULL_BLOCKS_PER_SM, EG_OPT_BATCH_WIDTH = 4, 5
 STATUS = {0: "EG_OK", 1: "EG_ERR_INVALID", 2: "EG_ERR_CUDA", 3: "EG_ERR_NOMEM", 4: "EG_ERR_STATE",
           5: "EG_ERR_TIMEOUT", 6: "EG_ERR_HOST_CALLBACK", 7: "EG_ERR_UNSUPPORTED"}
 
@@ -41,6 +42,16 @@ class Info(ctypes.Structure):
     _fields_ = [("V", ctypes.c_uint32), ("partitions", ctypes.c_uint32), ("E", ctypes.c_uint64),
                 ("ncompressed", ctypes.c_uint64), ("weighted", ctypes.c_int32), ("built_csr", ctypes.c_int32),
                 ("built_csc", ctypes.c_int32), ("symmetric", ctypes.c_int32)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("bfs_direction", ctypes.c_int32), ("dense_divisor", ctypes.c_int32),
+                ("pull_blocks_per_sm", ctypes.c_int32), ("cuda_graph", ctypes.c_int32), ("batch_width", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("bfs_ms", ctypes.c_double), ("pull_sweep_ms", ctypes.c_double),
+                ("msbfs_ms_per_root", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 class KernelStat(ctypes.Structure):
@@ -83,6 +94,8 @@ SIGNATURES = {
     "eg_load_directed_with_ids": ([_vp, _vp, _u64, _u32, _i32], _i32),
     "eg_ppr": ([_vp, _vp, _vp, _i32, _f32, _i32, _vp, _i32], _i32),
     "eg_ppr_backward": ([_vp, _vp, _vp, _i32, _f32, _i32, _vp, _vp, _i32], _i32),
+    "eg_bfs_many": ([_vp, _vp, _i32, _vp, _i32, _vp], _i32),
+    "eg_autotune": ([_vp, _vp, _i32, _vp], _i32),
     "eg_load_graph_batch": ([_vp, _vp, _i32, _vp, _vp, _i32, _i32], _i32),
     "eg_get_graph_batch": ([_vp, _vp, _vp], _i32),
     "eg_msbfs_graphs": ([_vp, _vp, _i32, _vp, _i32, _vp], _i32),
@@ -358,6 +371,20 @@ class Graph:
         _check(self._L.eg_ppr_backward(self.h, wp, sp, len(seeds), alpha, iterations, _buf(dl_dx)[0], _buf(dl_dw)[0],
                                        where))
         return dl_dw
+
+    def bfs_many(self, roots, levels=None):
+        roots = np.ascontiguousarray(roots, np.uint32)
+        p, where = _buf(levels)
+        rp = _buf(roots)[0] if where == EG_HOST else _buf(_to_device_u32(roots, levels))[0]
+        e = ctypes.c_uint64()
+        _check(self._L.eg_bfs_many(self.h, rp, len(roots), p, where, ctypes.byref(e)))
+        return levels, e.value
+
+    def autotune(self, sample_roots):
+        r = np.ascontiguousarray(sample_roots, np.uint32)
+        t = Tuning()
+        _check(self._L.eg_autotune(self.h, _buf(r)[0], len(r), ctypes.byref(t)))
+        return t.as_dict()
 
     def load_graph_batch(self, edges, graph_edges, graph_vertices):
         """edges: all graphs' records back to back; graph_edges[G+1]; graph_vertices[G]."""

@@ -442,6 +442,14 @@ int eg_set_option(eg_graph* g, int option, int64_t value) {
             if (value < 0 || value > 1) break;
             g->use_cuda_graph = (int)value;
             return EG_OK;
+        case EG_OPT_PULL_BLOCKS_PER_SM:
+            if (value < 0 || value > 64) break;
+            g->pull_blocks_per_sm = (int)value;
+            return EG_OK;
+        case EG_OPT_BATCH_WIDTH:
+            if (value < 1 || value > 64) break;
+            g->batch_width = (int)value;
+            return EG_OK;
         default:
             set_error("eg_set_option: unknown option %d", option);
             return EG_ERR_INVALID;

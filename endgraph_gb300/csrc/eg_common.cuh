@@ -174,6 +174,8 @@ struct eg_graph {
     int bfs_direction = 0;  // 0: Gemini threshold switch, 1: push only, 2: pull only
     int dense_div = 20;     // sparse iff active_edges < E / dense_div (core/graph.hpp:1491)
     int use_cuda_graph = 0; // batched BFS: replay the level loop as one captured CUDA graph
+    int pull_blocks_per_sm = 0;  // pull-sweep grid; 0 = occupancy limit
+    int batch_width = 64;        // roots per bit-parallel pass (eg_bfs_many)
     // many small graphs in one handle (eg_load_graph_batch): per-graph vertex / edge offsets
     std::vector<uint64_t> batch_voff, batch_eoff;
     eg::DevBuf d_batch_voff;

@@ -320,6 +320,7 @@ static int launch_pull(eg_graph* g, const Op& op, const char* name) {
     EG_CUDA(cudaFuncSetAttribute(k_pull<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<Op>, kPullThreads, smem));
+    if (g->pull_blocks_per_sm > 0) per_sm = std::min(per_sm, g->pull_blocks_per_sm);
     unsigned grid = (unsigned)std::min<uint64_t>(s.pull_nchunks, (uint64_t)g->num_sms * (uint64_t)std::max(per_sm, 1));
     Timed t(&g->prof, g->stream, name);
     k_pull<Op><<<grid, kPullThreads, smem, g->stream>>>(op, g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(),

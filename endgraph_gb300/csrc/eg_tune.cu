@@ -1,0 +1,161 @@
+// eg_tune.cu — project autotuner: times candidate engine settings on the loaded graph and keeps the
+// fastest (no reference counterpart; the reference hard-codes its switch at E/20 and its chunking).
+//
+//   dense divisor     process_edges runs sparse iff active out-edges < E / divisor (BFS), or
+//                     push-only as the reference's use_root mode
+//   pull CTAs per SM  grid of the chunked pull sweep (1, 2, 3, 4, or the occupancy limit)
+//   CUDA graph        batched BFS level loop replayed as a captured graph or driven from the host
+//   batch width       roots per bit-parallel pass in eg_bfs_many (16, 32 or 64)
+// Each candidate is timed as the median of three synchronous runs; settings are applied to the
+// handle and reported.
+#include <algorithm>
+#include <chrono>
+#include <vector>
+
+#include "eg_common.cuh"
+
+using namespace eg;
+
+namespace {
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+template <class F>
+int time_median(F f, double* ms) {
+    double t[3];
+    for (int i = 0; i < 3; ++i) {
+        const double a = now_ms();
+        const int s = f();
+        if (s != EG_OK) return s;
+        t[i] = now_ms() - a;
+    }
+    std::sort(t, t + 3);
+    *ms = t[1];
+    return EG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int eg_bfs_many(eg_graph* g, const uint32_t* roots, int nroots, uint8_t* levels, int where, uint64_t* edges) {
+    if (!g) { set_error("eg_bfs_many: null handle"); return EG_ERR_INVALID; }
+    if (!roots || nroots < 1) { set_error("eg_bfs_many: need roots"); return EG_ERR_INVALID; }
+    const int w = std::max(1, std::min(64, g->batch_width));
+    uint64_t total = 0;
+    std::vector<uint32_t> h(roots, roots + (where == EG_HOST ? nroots : 0));
+    if (where == EG_DEVICE) {
+        h.resize(nroots);
+        EG_CUDA(cudaMemcpy(h.data(), roots, 4ull * nroots, cudaMemcpyDeviceToHost));
+    }
+    for (int b = 0; b < nroots; b += w) {
+        const int n = std::min(w, nroots - b);
+        uint64_t e = 0;
+        uint8_t* out = levels ? levels + (size_t)b * g->V : nullptr;
+        EG_TRY(run_msbfs(g, h.data() + b, n, out, where, &e));
+        total += e;
+    }
+    if (edges) *edges = total;
+    g->last_edges_processed = total;
+    return EG_OK;
+}
+
+int eg_autotune(eg_graph* g, const uint32_t* sample_roots, int nroots, eg_tuning* out) {
+    if (!g || !sample_roots || nroots < 1 || !out) {
+        set_error("eg_autotune: need a handle, host sample roots and an output");
+        return EG_ERR_INVALID;
+    }
+    if (!g->built_csr || !g->built_csc) {
+        set_error("eg_autotune: graph not built");
+        return EG_ERR_STATE;
+    }
+    EG_CUDA(cudaSetDevice(g->device));
+    for (int i = 0; i < nroots; ++i)
+        if (sample_roots[i] >= g->V) {
+            set_error("eg_autotune: sample root %u >= V", sample_roots[i]);
+            return EG_ERR_INVALID;
+        }
+    const int nb = std::min(nroots, 4);
+    std::vector<uint32_t> r64(64);
+    for (int i = 0; i < 64; ++i) r64[i] = sample_roots[i % nroots];
+    memset(out, 0, sizeof(*out));
+
+    // 1. BFS direction switch
+    const int divs[] = {0, 5, 10, 20, 40, 100};  // 0: push only
+    double best = 1e30;
+    int best_div = g->dense_div, best_dir = g->bfs_direction;
+    for (int d : divs) {
+        g->bfs_direction = d == 0 ? 1 : 0;
+        if (d) g->dense_div = d;
+        double ms = 0;
+        EG_TRY(time_median([&]() {
+            for (int i = 0; i < nb; ++i) EG_TRY(run_bfs(g, sample_roots[i], nullptr, nullptr, EG_HOST, nullptr));
+            return (int)EG_OK;
+        }, &ms));
+        if (ms < best) {
+            best = ms;
+            best_div = d ? d : best_div;
+            best_dir = d == 0 ? 1 : 0;
+        }
+    }
+    g->bfs_direction = best_dir;
+    g->dense_div = best_div;
+    out->bfs_direction = best_dir;
+    out->dense_divisor = best_div;
+    out->bfs_ms = best / nb;
+
+    // 2. pull-sweep grid: CTAs per SM (0 = occupancy limit)
+    const int blocks[] = {0, 1, 2, 3, 4};
+    best = 1e30;
+    int best_blocks = 0;
+    for (int bps : blocks) {
+        g->pull_blocks_per_sm = bps;
+        double ms = 0;
+        EG_TRY(time_median([&]() { return run_pagerank(g, 2, 0.85f, nullptr, EG_HOST); }, &ms));
+        if (ms < best) {
+            best = ms;
+            best_blocks = bps;
+        }
+    }
+    g->pull_blocks_per_sm = best_blocks;
+    out->pull_blocks_per_sm = best_blocks;
+    out->pull_sweep_ms = best / 2;
+
+    // 3. captured level loop for batched BFS
+    best = 1e30;
+    int best_graph = 0;
+    for (int cg = 0; cg <= 1; ++cg) {
+        g->use_cuda_graph = cg;
+        EG_TRY(run_msbfs(g, r64.data(), 64, nullptr, EG_HOST, nullptr));  // capture outside the timing
+        double ms = 0;
+        EG_TRY(time_median([&]() { return run_msbfs(g, r64.data(), 64, nullptr, EG_HOST, nullptr); }, &ms));
+        if (ms < best) {
+            best = ms;
+            best_graph = cg;
+        }
+    }
+    g->use_cuda_graph = best_graph;
+    out->cuda_graph = best_graph;
+
+    // 4. roots per bit-parallel pass
+    const int widths[] = {16, 32, 64};
+    best = 1e30;
+    int best_w = 64;
+    for (int w : widths) {
+        g->batch_width = w;
+        double ms = 0;
+        EG_TRY(time_median([&]() { return eg_bfs_many(g, r64.data(), 64, nullptr, EG_HOST, nullptr); }, &ms));
+        if (ms < best) {
+            best = ms;
+            best_w = w;
+        }
+    }
+    g->batch_width = best_w;
+    out->batch_width = best_w;
+    out->msbfs_ms_per_root = best / 64;
+    return EG_OK;
+}
+
+}  // extern "C"

@@ -170,7 +170,13 @@ int eg_sssp(eg_graph* g, uint32_t root, float* dist, int where);
  * (core/graph.hpp:1496-1498), 2 forces pull.  Results are identical in every mode.
  * EG_OPT_CUDA_GRAPH: 1 replays the batched-BFS level loop (eg_msbfs, eg_msbfs_graphs) as one
  * captured CUDA graph of 32 levels instead of one host round trip per level. */
-enum { EG_OPT_BFS_DIRECTION = 1, EG_OPT_DENSE_DIVISOR = 2, EG_OPT_CUDA_GRAPH = 3 };
+enum {
+    EG_OPT_BFS_DIRECTION = 1,
+    EG_OPT_DENSE_DIVISOR = 2,
+    EG_OPT_CUDA_GRAPH = 3,
+    EG_OPT_PULL_BLOCKS_PER_SM = 4, /* pull-sweep CTAs per SM, 0 = occupancy limit */
+    EG_OPT_BATCH_WIDTH = 5         /* roots per bit-parallel pass of eg_bfs_many, 1..64 */
+};
 int eg_set_option(eg_graph* g, int option, int64_t value);
 
 /* ---- batched operators (no reference counterpart: batched forms of the toolkits) ---------- */
@@ -210,6 +216,26 @@ int eg_msbfs_graphs(eg_graph* g, const uint32_t* roots, int roots_per_graph, uin
 /* Bellman-Ford with sources_per_graph <= 64 sources in every graph (weighted batch):
  * dist[V_total][64] floats, row = union vertex, column = source index, 1e9 unreachable. */
 int eg_sssp_graphs(eg_graph* g, const uint32_t* sources, int sources_per_graph, float* dist, int where);
+
+/* BFS from many roots in bit-parallel passes of the tuned batch width (EG_OPT_BATCH_WIDTH, default
+ * 64): levels[nroots][V] bytes (may be NULL), *edges summed over roots. */
+int eg_bfs_many(eg_graph* g, const uint32_t* roots, int nroots, uint8_t* levels, int where, uint64_t* edges);
+
+/* Autotuner (no reference counterpart): times candidate settings on the built graph and keeps the
+ * fastest — BFS push/pull divisor or push-only, pull-sweep CTAs per SM, CUDA-graph replay of the
+ * batched BFS loop, and roots per bit-parallel pass.  sample_roots: host array. */
+typedef struct eg_tuning {
+    int32_t bfs_direction;      /* EG_OPT_BFS_DIRECTION chosen */
+    int32_t dense_divisor;      /* EG_OPT_DENSE_DIVISOR chosen */
+    int32_t pull_blocks_per_sm; /* EG_OPT_PULL_BLOCKS_PER_SM chosen (0: occupancy limit) */
+    int32_t cuda_graph;         /* EG_OPT_CUDA_GRAPH chosen */
+    int32_t batch_width;        /* EG_OPT_BATCH_WIDTH chosen */
+    int32_t reserved;
+    double bfs_ms;              /* best single-root BFS time */
+    double pull_sweep_ms;       /* best pull-sweep time (one PageRank iteration) */
+    double msbfs_ms_per_root;   /* best batched BFS time per root */
+} eg_tuning;
+int eg_autotune(eg_graph* g, const uint32_t* sample_roots, int nroots, eg_tuning* out);
 
 /* statistics of the last toolkit call: edges traversed, iterations, push / pull iterations */
 int eg_last_run(eg_graph* g, uint64_t* edges_processed, int* iterations, int* push_iters, int* pull_iters);

@@ -49,6 +49,27 @@ def test_msbfs_cuda_graph_mode(eg_lib, cuda_graph):
                 assert np.array_equal(levels[s], np.where(ref == oracle.UNREACHED, 255, ref).astype(np.uint8))
 
 
+def test_autotune_keeps_results(eg_lib):
+    """The tuner only changes how the work is scheduled: results after tuning equal the oracle."""
+    import endgraph_gb300 as eg
+    V, E = 1 << 15, 1 << 19
+    src, dst, _ = rmat_graph(V, E, 98)
+    csr = oracle.build_csr(src, dst, None, V, np.array([0, V], np.uint32))
+    roots = np.array(src[:70], np.uint32)
+    with eg.Graph() as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        t = g.autotune(roots[:8])
+        assert t["batch_width"] in (16, 32, 64) and t["cuda_graph"] in (0, 1)
+        assert t["bfs_ms"] > 0 and t["pull_sweep_ms"] > 0
+        lv, _ = g.bfs(int(roots[0]))
+        assert np.array_equal(lv, oracle.bfs_levels(csr["off"][0], csr["adj"], V, int(roots[0])))
+        levels = np.empty((70, V), np.uint8)
+        g.bfs_many(roots, levels)
+        for s in (0, 33, 69):
+            ref = oracle.bfs_levels(csr["off"][0], csr["adj"], V, int(roots[s]))
+            assert np.array_equal(levels[s], np.where(ref == oracle.UNREACHED, 255, ref).astype(np.uint8))
+
+
 def _graph_batch(G, seed, weighted=False):
     rng = np.random.default_rng(seed)
     Vs = np.exp(rng.uniform(np.log(100), np.log(5000), G)).astype(np.uint32)
