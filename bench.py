@@ -234,10 +234,17 @@ def run_batched(args, g, edges, roots, dev, stream):
     t_plain, e_plain = _timed(stream, plain_bfs)
     g.msbfs(roots, levels=lev64)
     t_ms, (_, e_ms) = _timed(stream, lambda: g.msbfs(roots, levels=lev64))
+    lr = g.last_run()
+    g.profile(True)
+    g.profile_reset()
+    g.msbfs(roots, levels=lev64)
+    g.profile(False)
+    kern = {k: round(ms, 3) for k, (n, ms) in sorted(g.profile_read().items(), key=lambda kv: -kv[1][1])}
     res["msbfs64"] = {"roots": 64, "plain_ms": round(t_plain, 3), "batched_ms": round(t_ms, 3),
                       "plain_gteps": round(e_plain / t_plain / 1e6, 2), "batched_gteps": round(e_ms / t_ms / 1e6, 2),
                       "speedup": round(t_plain / t_ms, 2), "same_edges": e_plain == e_ms,
-                      "sweeps": g.last_run()["iterations"]}
+                      "levels": lr["iterations"], "push_levels": lr["push"], "pull_levels": lr["pull"],
+                      "kernel_ms": kern}
     # personalised PageRank workload
     Vp = 1 << args.ppr_scale
     Ep = Vp * 16

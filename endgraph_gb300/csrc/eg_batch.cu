@@ -2,9 +2,9 @@
 // toolkits of toolkits/{bfs,sssp}.cpp and a personalised PageRank built on pagerank.cpp):
 //
 //  * eg_msbfs: bit-parallel BFS from up to 64 roots.  Every vertex keeps a u64 of the roots that
-//    reached it and a u64 of the roots whose frontier it is in; a level is one chunked pull over
-//    the CSC that ORs the in-neighbours' frontier words (exact integer work, levels identical to
-//    64 separate BFS runs).
+//    reached it and a u64 of the roots whose frontier it is in; a level either pushes the queued
+//    frontier's words along the CSR or is one chunked pull over the CSC that ORs the
+//    in-neighbours' frontier words (exact integer work, levels identical to 64 separate BFS runs).
 //  * 64-column row engine: a destination's 64 values (one per seed / source) sit in one 256-byte
 //    row; one warp reduces a task of <= kTaskEdges in-edges, each lane owning two columns, so every
 //    gathered row is a single coalesced 256-byte read.  Lists longer than a task are split and
@@ -32,50 +32,134 @@ constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 constexpr int kRowWarps = 8;  // 256-thread blocks
 
 // ---------------------------------------------------------------------------------------------
-// MS-BFS
-struct MsBfsPullOp {
+// MS-BFS.  A level is a pull sweep over the CSC when the frontier's out-edges reach E / divisor
+// (the switch of core/graph.hpp:1484-1491) and a push over the frontier queue otherwise.  Roots
+// whose traversal has ended can add nothing, so a destination whose visited word already holds
+// every root still running (`alive`) is skipped, and while the frontier is small a source outside
+// the frontier bitmap is not gathered at all.  The traversal kernels only set bits; the next
+// frontier is then listed once (k_bm_compact) and its level bytes written from that list
+// (k_queue_levels), so no traversal thread loops over the bits of a word.
+__device__ __forceinline__ bool bm_has(const unsigned long long* bm, uint32_t v) {
+    return (__ldg(bm + (v >> 6)) >> (v & 63)) & 1ull;
+}
+
+struct MsBfsPullOp {  // k_pull_direct operator
     using Acc = unsigned long long;
-    static constexpr bool kFilter = true;
+    const unsigned long long* front;
+    const unsigned long long* front_bm;  // 1 bit per vertex: front[v] != 0
+    int screen;                          // consult front_bm before gathering
+    unsigned long long* visit;
+    unsigned long long* next;
+    unsigned long long* next_bm;
+    const unsigned long long* alive;
+    const int* stop;  // captured level loops: set once a level found nothing new
+    __device__ bool stopped() const { return stop && *(volatile const int*)stop; }
+    __device__ bool item_active(uint32_t v) const {
+        const unsigned long long al = __ldg(alive);
+        return (__ldcg(visit + v) & al) != al;
+    }
+    __device__ Acc identity() const { return 0ull; }
+    __device__ Acc combine(Acc a, Acc b) const { return a | b; }
+    __device__ Acc gather(uint32_t u) const {
+        if (screen && !bm_has(front_bm, u)) return 0ull;
+        return __ldcg(front + u);
+    }
+    __device__ __forceinline__ void finish_direct(uint32_t v, Acc m) const {
+        const unsigned long long fresh = m & ~__ldcg(visit + v);
+        if (!fresh) return;
+        const unsigned long long nb = fresh & ~atomicOr(visit + v, fresh);
+        if (nb && atomicOr(next + v, nb) == 0ull) atomicOr(next_bm + (v >> 6), 1ull << (v & 63));
+    }
+};
+
+struct MsBfsPushOp {
     const unsigned long long* front;
     unsigned long long* visit;
     unsigned long long* next;
-    uint8_t* levels;  // [V][64], 0xFF = unreached
-    uint32_t next_level;
-    unsigned long long full;
-    uint32_t* n_new;
-    unsigned long long* reach_edges;
-    const uint32_t* deg;
-    const int* stop;  // captured level loops: set once a level found nothing new
-    __device__ bool stopped() const { return stop && *(volatile const int*)stop; }
-    __device__ bool item_active(uint32_t v) const { return __ldcg(visit + v) != full; }
-    __device__ Acc identity() const { return 0ull; }
-    __device__ Acc gather(uint32_t u, uint64_t) const { return __ldcg(front + u); }
-    __device__ Acc combine(Acc a, Acc b) const { return a | b; }
-    __device__ void smem_add(Acc* slot, Acc v) const {
-        if (v) atomicOr(slot, v);
-    }
-    __device__ void finish(bool ok, uint32_t v, Acc m, bool) const {
-        unsigned long long nb = 0;
-        if (ok && m) {
-            const unsigned long long old = atomicOr(visit + v, m);
-            nb = m & ~old;
-            if (nb) {
-                atomicOr(next + v, nb);
-                atomicAdd(reach_edges, (unsigned long long)__popcll(nb) * deg[v]);
-                if (levels) {
-                    unsigned long long b = nb;
-                    while (b) {
-                        const int s = __ffsll((long long)b) - 1;
-                        b &= b - 1;
-                        levels[(uint64_t)v * 64 + s] = (uint8_t)next_level;
-                    }
-                }
-            }
-        }
-        const unsigned any = __ballot_sync(0xffffffffu, nb != 0);
-        if ((threadIdx.x & 31) == 0 && any) atomicAdd(n_new, (uint32_t)__popc(any));
+    unsigned long long* next_bm;
+    __device__ unsigned long long payload(uint32_t u) const { return __ldcg(front + u); }
+    __device__ bool relax(uint32_t, unsigned long long pay, uint32_t w, uint64_t) const {
+        const unsigned long long m = pay & ~__ldcg(visit + w);
+        if (!m) return false;
+        const unsigned long long nb = m & ~atomicOr(visit + w, m);
+        if (!nb || atomicOr(next + w, nb) != 0ull) return false;
+        atomicOr(next_bm + (w >> 6), 1ull << (w & 63));
+        return true;  // w joins the next frontier's queue
     }
 };
+
+// next frontier bitmap -> vertex queue, its length and the out-edges of the queued vertices;
+// one warp per 32 words
+__global__ void k_bm_compact(const unsigned long long* __restrict__ bm, uint64_t nwords, uint32_t* q, uint32_t* nq,
+                             unsigned long long* act_edges, const uint32_t* __restrict__ deg) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < nwords; base += stride) {
+        const uint64_t w = base + lane;
+        unsigned long long word = w < nwords ? bm[w] : 0ull;
+        const uint32_t cnt = (uint32_t)__popcll(word);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+        if (!tot) continue;
+        uint32_t at = 0;
+        if (lane == 31) at = atomicAdd(nq, tot);
+        at = __shfl_sync(0xffffffffu, at, 31) + incl - cnt;
+        unsigned long long d = 0;
+        while (word) {
+            const uint32_t v = (uint32_t)(w * 64 + (uint64_t)(__ffsll((long long)word) - 1));
+            word &= word - 1;
+            q[at++] = v;
+            d += deg[v];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if (lane == 0 && act_edges && d) atomicAdd(act_edges, d);
+    }
+}
+
+// level bytes of the queued vertices' new bits (row v of [V][64]: 16 threads, one 4-byte word
+// each) and the OR of their words, i.e. the roots whose traversal is still running
+__global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n_dev,
+                               const unsigned long long* __restrict__ next, uint8_t* levels, uint32_t lvl,
+                               unsigned long long* alive_out) {
+    const uint32_t n = __ldcg(n_dev);
+    const uint32_t sub = threadIdx.x & 15;
+    const uint32_t fill = (lvl & 0xFFu) * 0x01010101u;
+    unsigned long long orr = 0;
+    for (uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 4; i < n;
+         i += ((uint64_t)gridDim.x * blockDim.x) >> 4) {
+        const uint32_t v = q[i];
+        const unsigned long long nb = next[v];
+        orr |= nb;
+        const uint32_t nib = (uint32_t)(nb >> (4 * sub)) & 0xFu;
+        if (levels && nib) {
+            // bit k of the nibble -> byte k all ones (the four shifted copies never overlap)
+            const uint32_t m = ((nib * 0x00204081u) & 0x01010101u) * 0xFFu;
+            uint32_t* p = reinterpret_cast<uint32_t*>(levels + (uint64_t)v * 64) + sub;
+            *p = (*p & ~m) | (fill & m);
+        }
+    }
+    if (!alive_out) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) orr |= __shfl_xor_sync(0xffffffffu, orr, o);
+    if ((threadIdx.x & 31) == 0 && orr) atomicOr(alive_out, orr);
+}
+
+// sum over vertices of popcount(visited word) * out-degree: the edges 64 single-root runs scan
+__global__ void k_reach_edges(const unsigned long long* __restrict__ visit, const uint32_t* __restrict__ deg, uint64_t V,
+                              unsigned long long* out) {
+    unsigned long long acc = 0;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x)
+        acc += (unsigned long long)__popcll(visit[v]) * deg[v];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
 
 // [V][64] -> [n][V] for the first n columns (32x32 tiles through shared memory)
 __global__ void k_transpose_u8(const uint8_t* __restrict__ in, uint32_t V, int n, uint8_t* __restrict__ out) {
@@ -411,7 +495,7 @@ int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E) {
 // ---------------------------------------------------------------------------------------------
 struct BatchState {
     DevBuf a64, b64, c64, lev, rows0, rows1, heavy, tmp_out, seeds, wn_csc, wn_csr, s_out, gA, row_of, ck, seg;
-    DevBuf ch0, ch1, flag, level_cnt, entries, n_entries;
+    DevBuf ch0, ch1, flag, level_cnt, entries, n_entries, bm0, bm1, alive;
     RowTasks csc_tasks, csr_tasks;
     bool csc_ready = false, csr_ready = false;
     // captured MS-BFS level loop and the shapes it was captured for
@@ -475,18 +559,19 @@ __global__ void k_root_entries_graphs(const uint32_t* roots, const uint64_t* vof
 }
 
 __global__ void k_msbfs_init_entries(const uint2* ent, const uint32_t* n_dev, unsigned long long* visit,
-                                     unsigned long long* front, uint8_t* levels, unsigned long long* reach_edges,
-                                     const uint32_t* deg) {
+                                     unsigned long long* front, unsigned long long* front_bm, uint8_t* levels,
+                                     uint32_t* q, uint32_t* nq, unsigned long long* act_edges, const uint32_t* deg) {
     const uint32_t n = *n_dev;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t v = ent[i].x, s = ent[i].y;
         const unsigned long long bit = 1ull << s;
         const unsigned long long old = atomicOr(visit + v, bit);
-        atomicOr(front + v, bit);
-        if (!(old & bit)) {
-            if (levels) levels[(uint64_t)v * 64 + s] = 0;
-            atomicAdd(reach_edges, (unsigned long long)deg[v]);
+        if (atomicOr(front + v, bit) == 0ull) {
+            atomicOr(front_bm + (v >> 6), 1ull << (v & 63));
+            q[atomicAdd(nq, 1u)] = v;
+            atomicAdd(act_edges, (unsigned long long)deg[v]);
         }
+        if (!(old & bit) && levels) levels[(uint64_t)v * 64 + s] = 0;
     }
 }
 
@@ -498,39 +583,75 @@ __global__ void k_level_gate(const uint32_t* prev_new, int* stop) {
 constexpr int kGraphLevels = 32;
 
 // MS-BFS over root entries already in b.entries (count in b.n_entries device word)
-static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, uint64_t* reach_out, int* sweeps_out) {
+static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, uint64_t* reach_out, int* sweeps_out,
+                      int* pushes_out) {
     BatchState& b = bstate(g);
+    EngineState& s = g->eng;
     const uint64_t V = g->V;
+    const uint64_t nwords = V / 64 + 1;
+    const size_t bm_bytes = 8 * nwords;
     unsigned long long* visit = b.a64.as<unsigned long long>();
-    unsigned long long* bufA = b.b64.as<unsigned long long>();
-    unsigned long long* bufB = b.c64.as<unsigned long long>();
+    unsigned long long* word[2] = {b.b64.as<unsigned long long>(), b.c64.as<unsigned long long>()};
+    unsigned long long* bm[2] = {b.bm0.as<unsigned long long>(), b.bm1.as<unsigned long long>()};
+    uint32_t* queue[2] = {s.q0.as<uint32_t>(), s.q1.as<uint32_t>()};
+    unsigned long long* alive = b.alive.as<unsigned long long>();  // [0..1] per level parity, [2] all roots
     uint32_t* cnt = b.level_cnt.as<uint32_t>();  // [kGraphLevels + 1]
     int* stop = reinterpret_cast<int*>(cnt + kGraphLevels + 1);
-    unsigned long long* d_reach = g->eng.counters.as<unsigned long long>() + 4;
+    unsigned long long* d_reach = s.counters.as<unsigned long long>() + 4;
+    uint32_t* d_nq = reinterpret_cast<uint32_t*>(s.counters.as<unsigned long long>() + 2);
+    unsigned long long* d_act = s.counters.as<unsigned long long>() + 3;
     const unsigned long long full = nbits == 64 ? ~0ull : ((1ull << nbits) - 1ull);
     const uint32_t* deg = g->outdeg.as<uint32_t>();
     const unsigned init_grid = std::max(1u, std::min<unsigned>((n_entries + 255) / 256, 4096u));
+    const unsigned grid = (unsigned)g->num_sms * 8u;
 
     auto enqueue_init = [&]() -> int {
         EG_CUDA(cudaMemsetAsync(visit, 0, 8 * V, g->stream));
-        EG_CUDA(cudaMemsetAsync(bufA, 0, 8 * V, g->stream));
-        EG_CUDA(cudaMemsetAsync(d_reach, 0, 8, g->stream));
+        EG_CUDA(cudaMemsetAsync(word[0], 0, 8 * V, g->stream));
+        EG_CUDA(cudaMemsetAsync(bm[0], 0, bm_bytes, g->stream));
+        EG_CUDA(cudaMemsetAsync(d_nq, 0, 16, g->stream));
         EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (kGraphLevels + 2), g->stream));
+        EG_CUDA(cudaMemcpyAsync(alive + 2, &full, 8, cudaMemcpyHostToDevice, g->stream));
+        EG_CUDA(cudaMemcpyAsync(alive, &full, 8, cudaMemcpyHostToDevice, g->stream));
         if (lev) EG_CUDA(cudaMemsetAsync(lev, 0xFF, 64 * V, g->stream));
         k_msbfs_init_entries<<<init_grid, 256, 0, g->stream>>>(b.entries.as<uint2>(), b.n_entries.as<uint32_t>(), visit,
-                                                               bufA, lev, d_reach, deg);
+                                                               word[0], bm[0], lev, queue[0], d_nq, d_act, deg);
         EG_CHECK_LAUNCH("k_msbfs_init_entries");
         return EG_OK;
     };
-    auto enqueue_level = [&](uint32_t lvl, uint32_t* counter, const int* stop_flag) -> int {
-        unsigned long long* front = (lvl & 1) ? bufB : bufA;
-        unsigned long long* next = (lvl & 1) ? bufA : bufB;
-        EG_CUDA(cudaMemsetAsync(next, 0, 8 * V, g->stream));
-        MsBfsPullOp op{front, visit, next, lev, lvl + 1, full, counter, d_reach, deg, stop_flag};
-        return launch_pull(g, op, "msbfs_pull");
+    // one level L: frontier word[L&1] / bm[L&1] / queue[L&1] -> the same of parity (L+1)&1.  The
+    // queue length lands in *count; captured loops (stop_flag set) pull every level and keep the
+    // alive mask at "all roots".
+    auto enqueue_level = [&](uint32_t L, uint64_t n_host, bool dense, bool screen, uint32_t* count, const int* stop_flag,
+                             uint32_t* nout_host, unsigned long long* act_host) -> int {
+        const int c = L & 1, x = c ^ 1;
+        EG_CUDA(cudaMemsetAsync(word[x], 0, 8 * V, g->stream));
+        EG_CUDA(cudaMemsetAsync(bm[x], 0, bm_bytes, g->stream));
+        unsigned long long* alive_next = stop_flag ? nullptr : alive + x;
+        if (alive_next) EG_CUDA(cudaMemsetAsync(alive_next, 0, 8, g->stream));
+        if (dense) {
+            EG_CUDA(cudaMemsetAsync(count, 0, 4, g->stream));
+            if (!stop_flag) EG_CUDA(cudaMemsetAsync(d_act, 0, 8, g->stream));
+            MsBfsPullOp op{word[c], bm[c], screen ? 1 : 0, visit, word[x], bm[x], stop_flag ? alive + 2 : alive + c,
+                           stop_flag};
+            EG_TRY(launch_pull_direct(g, op, "msbfs_pull"));
+            Timed t(&g->prof, g->stream, "msbfs_vertex");
+            k_bm_compact<<<grid_for(nwords, 256, grid), 256, 0, g->stream>>>(bm[x], nwords, queue[x], count,
+                                                                            stop_flag ? nullptr : d_act, deg);
+            EG_CHECK_LAUNCH("k_bm_compact");
+        } else {
+            MsBfsPushOp op{word[c], visit, word[x], bm[x]};
+            EG_TRY(push_level(g, op, queue[c], n_host, queue[x], nout_host, nullptr, act_host, deg, "msbfs_push"));
+        }
+        if (lev || alive_next) {
+            Timed t(&g->prof, g->stream, "msbfs_vertex");
+            k_queue_levels<<<grid, 256, 0, g->stream>>>(queue[x], count, word[x], lev, L + 1, alive_next);
+            EG_CHECK_LAUNCH("k_queue_levels");
+        }
+        return EG_OK;
     };
 
-    int sweeps = 0;
+    int sweeps = 0, pushes = 0;
     uint32_t lvl = 0;
     if (g->use_cuda_graph) {
         // init + kGraphLevels levels replayed as one CUDA graph; levels after an empty one stop at
@@ -549,7 +670,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
                     k_level_gate<<<1, 1, 0, g->stream>>>(cnt + L - 1, stop);
                     st = cudaGetLastError() == cudaSuccess ? EG_OK : EG_ERR_CUDA;
                 }
-                if (st == EG_OK) st = enqueue_level(L, cnt + L, stop);
+                if (st == EG_OK) st = enqueue_level(L, 0, true, true, cnt + L, stop, nullptr, nullptr);
             }
             cudaGraph_t graph = nullptr;
             cudaError_t e = cudaStreamEndCapture(g->stream, &graph);
@@ -573,36 +694,70 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         std::vector<uint32_t> h(kGraphLevels);
         EG_CUDA(cudaMemcpyAsync(h.data(), cnt, sizeof(uint32_t) * kGraphLevels, cudaMemcpyDeviceToHost, g->stream));
         EG_CUDA(cudaStreamSynchronize(g->stream));
-        for (int L = 0; L < kGraphLevels; ++L) {
+        bool done = false;
+        for (int L = 0; L < kGraphLevels && !done; ++L) {
             ++sweeps;
-            if (h[L] == 0) break;
+            done = h[L] == 0;
         }
-        if (h[kGraphLevels - 1] == 0) {
-            if (reach_out) EG_CUDA(cudaMemcpy(reach_out, d_reach, 8, cudaMemcpyDeviceToHost));
-            *sweeps_out = sweeps;
-            return EG_OK;
+        lvl = kGraphLevels;
+        uint32_t* d_new = cnt + kGraphLevels;
+        while (!done) {  // deeper than the captured levels
+            if (lvl >= 254) {
+                set_error("eg_msbfs: more than 254 levels");
+                return EG_ERR_UNSUPPORTED;
+            }
+            EG_TRY(enqueue_level(lvl, 0, true, true, d_new, stop, nullptr, nullptr));
+            ++sweeps;
+            uint32_t hn = 0;
+            EG_CUDA(cudaMemcpyAsync(&hn, d_new, 4, cudaMemcpyDeviceToHost, g->stream));
+            EG_CUDA(cudaStreamSynchronize(g->stream));
+            done = hn == 0;
+            ++lvl;
         }
-        lvl = kGraphLevels;  // deeper than the captured levels: continue below
     } else {
         EG_TRY(enqueue_init());
-    }
-    uint32_t* d_new = cnt + kGraphLevels;
-    while (true) {
-        if (lvl >= 254) {
-            set_error("eg_msbfs: more than 254 levels");
-            return EG_ERR_UNSUPPORTED;
-        }
-        EG_CUDA(cudaMemsetAsync(d_new, 0, 4, g->stream));
-        EG_TRY(enqueue_level(lvl, d_new, nullptr));
-        ++sweeps;
-        uint32_t h = 0;
-        EG_CUDA(cudaMemcpyAsync(&h, d_new, 4, cudaMemcpyDeviceToHost, g->stream));
+        struct {
+            uint32_t n;
+            uint32_t pad;
+            unsigned long long act;
+        } h;
+        EG_CUDA(cudaMemcpyAsync(&h, d_nq, 16, cudaMemcpyDeviceToHost, g->stream));
         EG_CUDA(cudaStreamSynchronize(g->stream));
-        if (!h) break;
-        ++lvl;
+        uint64_t n = h.n;
+        unsigned long long act = h.act;
+        while (n > 0) {
+            if (lvl >= 254) {
+                set_error("eg_msbfs: more than 254 levels");
+                return EG_ERR_UNSUPPORTED;
+            }
+            const bool dense = !g->built_csr || g->bfs_direction == 2 ||
+                               (g->bfs_direction == 0 && act >= g->E / (uint64_t)g->dense_div);
+            uint32_t nout = 0;
+            // a bitmap test before each gather pays only while the frontier is a small part of V
+            EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act));
+            if (dense) {
+                EG_CUDA(cudaMemcpyAsync(&h, d_nq, 16, cudaMemcpyDeviceToHost, g->stream));
+                EG_CUDA(cudaStreamSynchronize(g->stream));
+                nout = h.n;
+                act = h.act;
+            } else {
+                ++pushes;
+            }
+            ++sweeps;
+            n = nout;
+            ++lvl;
+        }
     }
-    if (reach_out) EG_CUDA(cudaMemcpy(reach_out, d_reach, 8, cudaMemcpyDeviceToHost));
+    if (reach_out) {
+        EG_CUDA(cudaMemsetAsync(d_reach, 0, 8, g->stream));
+        Timed t(&g->prof, g->stream, "msbfs_vertex");
+        k_reach_edges<<<grid_for(V, 256, grid), 256, 0, g->stream>>>(visit, deg, V, d_reach);
+        EG_CHECK_LAUNCH("k_reach_edges");
+        EG_CUDA(cudaMemcpyAsync(reach_out, d_reach, 8, cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaStreamSynchronize(g->stream));
+    }
     *sweeps_out = sweeps;
+    if (pushes_out) *pushes_out = pushes;
     return EG_OK;
 }
 
@@ -615,6 +770,9 @@ static int msbfs_buffers(eg_graph* g, uint32_t n_entries, bool with_levels) {
     EG_TRY(b.b64.reserve(8 * V + 8));
     EG_TRY(b.c64.reserve(8 * V + 8));
     EG_TRY(b.level_cnt.reserve(sizeof(uint32_t) * (kGraphLevels + 4)));
+    EG_TRY(b.bm0.reserve(8 * (V / 64 + 1)));
+    EG_TRY(b.bm1.reserve(8 * (V / 64 + 1)));
+    EG_TRY(b.alive.reserve(64));
     EG_TRY(b.entries.reserve(sizeof(uint2) * (n_entries + 1)));
     EG_TRY(b.n_entries.reserve(16));
     if (with_levels) EG_TRY(b.lev.reserve(64 * V + 64));
@@ -633,8 +791,8 @@ int run_msbfs(eg_graph* g, const uint32_t* roots, int n, uint8_t* levels, int wh
     EG_CHECK_LAUNCH("k_root_entries");
     uint8_t* lev = levels ? b.lev.as<uint8_t>() : nullptr;
     uint64_t reach = 0;
-    int sweeps = 0;
-    EG_TRY(msbfs_core(g, (uint32_t)n, n, lev, &reach, &sweeps));
+    int sweeps = 0, pushes = 0;
+    EG_TRY(msbfs_core(g, (uint32_t)n, n, lev, &reach, &sweeps, &pushes));
     if (levels) {
         uint8_t* out = levels;
         if (where != EG_DEVICE) {
@@ -651,8 +809,8 @@ int run_msbfs(eg_graph* g, const uint32_t* roots, int n, uint8_t* levels, int wh
     if (edges) *edges = reach;
     g->last_edges_processed = reach;
     g->last_iterations = sweeps;
-    g->last_pushes = 0;
-    g->last_pulls = sweeps;
+    g->last_pushes = pushes;
+    g->last_pulls = sweeps - pushes;
     return EG_OK;
 }
 
@@ -1082,8 +1240,8 @@ int run_msbfs_graphs(eg_graph* g, const uint32_t* roots, int nper, uint8_t* leve
     BatchState& b = bstate(g);
     EG_CUDA(cudaMemcpyAsync(b.n_entries.ptr, &n, 4, cudaMemcpyHostToDevice, g->stream));
     uint64_t reach = 0;
-    int sweeps = 0;
-    EG_TRY(msbfs_core(g, n, nper, levels ? b.lev.as<uint8_t>() : nullptr, &reach, &sweeps));
+    int sweeps = 0, pushes = 0;
+    EG_TRY(msbfs_core(g, n, nper, levels ? b.lev.as<uint8_t>() : nullptr, &reach, &sweeps, &pushes));
     if (levels)
         EG_CUDA(cudaMemcpyAsync(levels, b.lev.ptr, 64ull * g->V,
                                 where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, g->stream));
@@ -1091,8 +1249,8 @@ int run_msbfs_graphs(eg_graph* g, const uint32_t* roots, int nper, uint8_t* leve
     if (edges) *edges = reach;
     g->last_edges_processed = reach;
     g->last_iterations = sweeps;
-    g->last_pulls = sweeps;
-    g->last_pushes = 0;
+    g->last_pulls = sweeps - pushes;
+    g->last_pushes = pushes;
     return EG_OK;
 }
 

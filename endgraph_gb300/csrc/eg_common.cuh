@@ -113,6 +113,7 @@ struct EngineState {
     DevBuf vals0, vals1;   // per-vertex values
     DevBuf pull_chunk_item;  // u32 per CSC chunk: first compressed item
     DevBuf pull_split;     // u32 list of vertices whose list spans a chunk boundary
+    DevBuf bu_seg;         // u64 segments of the early-exit dense BFS step
     uint64_t pull_nsplit = 0;
     uint64_t pull_nchunks = 0;
     bool pull_ready = false;

@@ -38,13 +38,20 @@ struct BfsOp {  // toolkits/bfs.cpp:52-58: first visitor of dst becomes its pare
     }
 };
 
-// dense BFS step (toolkits/bfs.cpp:60-76): an unvisited destination takes an in-neighbour that is
-// in the current frontier as its parent (here the smallest one seen by a chunk); destinations that
-// are already visited are filtered out before their in-lists are read
-struct BfsPullOp {
-    using Acc = uint32_t;
-    static constexpr bool kFilter = true;
-    __device__ bool stopped() const { return false; }
+// dense BFS step (toolkits/bfs.cpp:60-76): every unvisited destination looks for an in-neighbour
+// in the current frontier and stops at the first one, which becomes its parent.  Stage one gives
+// each compressed CSC entry a thread that reads at most kBuHead in-edges; an entry with a longer
+// list that found nothing there is cut into kBuSeg-edge segments, and in stage two a warp reads a
+// segment 128 ids per step and leaves as soon as any segment of that destination has claimed it.
+constexpr uint32_t kBuHead = 8;
+constexpr uint32_t kBuSeg = 1024;
+
+struct BuArgs {
+    const uint32_t* adj;
+    const uint64_t* cidx;
+    const uint32_t* cvert;
+    uint64_t nitems;
+    uint32_t V;
     const unsigned long long* front;
     unsigned long long* visited;
     unsigned long long* next_front;
@@ -55,29 +62,98 @@ struct BfsPullOp {
     uint32_t* n_out;
     unsigned long long* act_edges;
     const uint32_t* deg;
-    __device__ bool item_active(uint32_t v) const { return !((__ldcg(visited + (v >> 6)) >> (v & 63)) & 1ull); }
-    __device__ Acc identity() const { return 0xFFFFFFFFu; }
-    __device__ Acc gather(uint32_t u, uint64_t) const {
-        return ((__ldg(front + (u >> 6)) >> (u & 63)) & 1ull) ? u : 0xFFFFFFFFu;
-    }
-    __device__ Acc combine(Acc a, Acc b) const { return a < b ? a : b; }
-    __device__ void smem_add(Acc* slot, Acc v) const {
-        if (v != 0xFFFFFFFFu) atomicMin(slot, v);
-    }
-    __device__ void finish(bool ok, uint32_t v, Acc m, bool) const {
+    unsigned long long* seg;  // (segment << 32) | compressed entry
+    uint32_t* nseg;
+};
+
+__device__ __forceinline__ bool bu_in_front(const BuArgs& a, uint32_t u) {
+    return (__ldg(a.front + (u >> 6)) >> (u & 63)) & 1ull;
+}
+__device__ __forceinline__ bool bu_claim(const BuArgs& a, uint32_t v, uint32_t par) {
+    const unsigned long long bit = 1ull << (v & 63);
+    if (atomicOr(a.visited + (v >> 6), bit) & bit) return false;  // another entry of v won
+    if (a.level) a.level[v] = a.next_level;
+    if (a.parent) a.parent[v] = par;
+    atomicOr(a.next_front + (v >> 6), bit);
+    return true;
+}
+
+__global__ void __launch_bounds__(256) k_bu_head(BuArgs a) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.nitems; base += stride) {
+        const uint64_t i = base + threadIdx.x;
         bool act = false;
-        if (ok && m != 0xFFFFFFFFu) {
-            const unsigned long long bit = 1ull << (v & 63);
-            if (!(atomicOr(visited + (v >> 6), bit) & bit)) {
-                if (level) level[v] = next_level;
-                if (parent) parent[v] = m;
-                atomicOr(next_front + (v >> 6), bit);
-                act = true;
+        uint32_t v = a.V, nsg = 0;
+        if (i < a.nitems) {
+            v = a.cvert[i];
+            if (v < a.V && !((__ldcg(a.visited + (v >> 6)) >> (v & 63)) & 1ull)) {
+                const uint64_t s = a.cidx[i], e = a.cidx[i + 1];
+                const uint64_t h = e - s > kBuHead ? s + kBuHead : e;
+                uint32_t par = 0xFFFFFFFFu;
+                for (uint64_t p = s; p < h; ++p) {
+                    const uint32_t u = __ldg(a.adj + p);
+                    if (bu_in_front(a, u)) {
+                        par = u;
+                        break;
+                    }
+                }
+                if (par != 0xFFFFFFFFu) act = bu_claim(a, v, par);
+                else if (e > h) nsg = (uint32_t)((e - h + kBuSeg - 1) / kBuSeg);
             }
         }
-        append_active(act, v, q_out, n_out, act_edges, deg);
+        append_active(act, v, a.q_out, a.n_out, a.act_edges, a.deg);
+        uint32_t incl = nsg;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+        if (tot) {
+            uint32_t at = 0;
+            if (lane == 31) at = atomicAdd(a.nseg, tot);
+            at = __shfl_sync(0xffffffffu, at, 31) + incl - nsg;
+            for (uint32_t k = 0; k < nsg; ++k) a.seg[at + k] = ((unsigned long long)k << 32) | (uint32_t)i;
+        }
     }
-};
+}
+
+__global__ void __launch_bounds__(256) k_bu_tail(BuArgs a) {
+    const uint32_t n = __ldcg(a.nseg);
+    const int lane = threadIdx.x & 31;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < n; t += nwarps) {
+        const unsigned long long ent = a.seg[t];
+        const uint32_t i = (uint32_t)ent;
+        const uint32_t v = a.cvert[i];
+        const uint64_t e = a.cidx[i + 1];
+        uint64_t p = a.cidx[i] + kBuHead + (ent >> 32) * kBuSeg;
+        const uint64_t pe = p + kBuSeg < e ? p + kBuSeg : e;
+        const unsigned long long bit = 1ull << (v & 63);
+        bool act = false;
+        for (; p < pe; p += 128) {
+            if (__any_sync(0xffffffffu, (__ldcg(a.visited + (v >> 6)) & bit) != 0)) break;
+            uint32_t u[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint64_t x = p + 32 * q + lane;
+                u[q] = x < pe ? __ldg(a.adj + x) : 0xFFFFFFFFu;
+            }
+            uint32_t cand = 0xFFFFFFFFu;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (cand == 0xFFFFFFFFu && u[q] != 0xFFFFFFFFu && bu_in_front(a, u[q])) cand = u[q];
+            const unsigned m = __ballot_sync(0xffffffffu, cand != 0xFFFFFFFFu);
+            if (m) {
+                const uint32_t par = __shfl_sync(0xffffffffu, cand, __ffs(m) - 1);
+                if (lane == 0) act = bu_claim(a, v, par);
+                break;
+            }
+        }
+        append_active(act, v, a.q_out, a.n_out, a.act_edges, a.deg);
+    }
+}
 
 struct SsspOp {  // toolkits/sssp.cpp:52-64: relax_dist = dist[src] + w; write_min
     float* dist;
@@ -322,7 +398,13 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
     unsigned long long active_edges = root_deg, total_edges = root_deg;
     uint32_t lvl = 0;
     int pushes = 0, pulls = 0;
-    if (g->built_csc) EG_TRY(setup_pull(g));
+    if (g->built_csc) {
+        // segment list of the dense step: at most one segment per entry with more than kBuHead
+        // in-edges plus one per kBuSeg edges
+        const uint64_t nitems = g->ncompressed - 1;
+        const uint64_t heavy = std::min<uint64_t>(nitems, g->E / (kBuHead + 1));
+        EG_TRY(s.bu_seg.reserve(sizeof(unsigned long long) * (heavy + g->E / kBuSeg + 2)));
+    }
     while (n > 0) {
         // core/graph.hpp:1484-1491 (Gemini's switch): sparse iff the frontier's out-edges < E / div
         const bool dense = g->bfs_direction == 2 ||
@@ -336,10 +418,22 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
         } else {
             uint32_t* d_nout = reinterpret_cast<uint32_t*>(s.counters.as<unsigned long long>() + 2);
             unsigned long long* d_act = s.counters.as<unsigned long long>() + 3;
+            uint32_t* d_nseg = reinterpret_cast<uint32_t*>(s.counters.as<unsigned long long>() + 5);
             EG_CUDA(cudaMemsetAsync(d_nout, 0, 16, g->stream));
-            BfsPullOp op{front, s.bm_visit.as<unsigned long long>(), next_front, d_level, d_parent, lvl + 1, qb, d_nout,
-                         d_act, g->outdeg.as<uint32_t>()};
-            EG_TRY(launch_pull(g, op, "bfs_pull"));
+            EG_CUDA(cudaMemsetAsync(d_nseg, 0, 8, g->stream));
+            BuArgs a{g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(), g->ncompressed - 1, V,
+                     front, s.bm_visit.as<unsigned long long>(), next_front, d_level, d_parent, lvl + 1, qb, d_nout,
+                     d_act, g->outdeg.as<uint32_t>(), s.bu_seg.as<unsigned long long>(), d_nseg};
+            {
+                Timed t(&g->prof, g->stream, "bfs_pull");
+                k_bu_head<<<grid_for(a.nitems, 256, (unsigned)g->num_sms * 8u), 256, 0, g->stream>>>(a);
+                EG_CHECK_LAUNCH("k_bu_head");
+            }
+            {
+                Timed t(&g->prof, g->stream, "bfs_pull_tail");
+                k_bu_tail<<<(unsigned)g->num_sms * 8u, 256, 0, g->stream>>>(a);
+                EG_CHECK_LAUNCH("k_bu_tail");
+            }
             struct {
                 uint32_t n;
                 uint32_t pad;

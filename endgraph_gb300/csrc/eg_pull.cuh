@@ -179,6 +179,128 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
     }
 }
 
+// Pull without shared accumulators, for operators whose reduction is an idempotent OR that may be
+// applied to a destination in pieces (Op::finish_direct(v, part) any number of times per level).
+// One CTA per chunk: the chunk's item boundaries and filtered destinations are staged in shared
+// memory (6 bytes per item, so eight CTAs fit an SM); a segment closed inside a thread's 16 edges
+// is applied at once, and the open segments at the ends of threads are merged along the warp
+// first.  No second barrier, so CTAs retire as soon as their own chunk is done.
+template <class Op>
+__global__ void __launch_bounds__(kPullThreads) k_pull_direct(Op op, const uint32_t* __restrict__ adj,
+                                                               const uint64_t* __restrict__ cidx,
+                                                               const uint32_t* __restrict__ cvert,
+                                                               const uint32_t* __restrict__ chunk_item, uint64_t E,
+                                                               uint64_t nitems, uint32_t V) {
+    using Acc = typename Op::Acc;
+    if (op.stopped()) return;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const uint64_t c = blockIdx.x;
+    const uint64_t e0 = c * kPullChunk;
+    const uint64_t e1 = e0 + kPullChunk < E ? e0 + kPullChunk : E;
+    const uint32_t i0 = chunk_item[c];
+    const uint32_t j = chunk_item[c + 1];
+    const uint32_t iend = (j < nitems && cidx[j] < e1) ? j + 1 : j;
+    const int nit = (int)(iend - i0);
+    uint32_t* s_v = reinterpret_cast<uint32_t*>(s_raw);    // destination, or ~0u when filtered out
+    uint16_t* s_idx = reinterpret_cast<uint16_t*>(s_v + nit);  // nit + 1 boundaries relative to e0
+    for (int k = threadIdx.x; k <= nit; k += blockDim.x) {
+        const uint64_t x = cidx[i0 + k];
+        s_idx[k] = (uint16_t)(x <= e0 ? 0u : (x >= e1 ? (uint32_t)(e1 - e0) : (uint32_t)(x - e0)));
+        if (k < nit) {
+            const uint32_t v = cvert[i0 + k];
+            s_v[k] = (v < V && op.item_active(v)) ? v : 0xFFFFFFFFu;
+        }
+    }
+    __syncthreads();
+    const uint64_t eb = e0 + (uint64_t)threadIdx.x * kPullPerThread;
+    const uint32_t rb = (uint32_t)(eb - e0);
+    int fin_key = 0x7fffffff;
+    Acc fin = op.identity();
+    if (eb < e1) {
+        int lo = 0, hi = nit;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (s_idx[mid] <= rb) lo = mid; else hi = mid;
+        }
+        const uint64_t ee = eb + kPullPerThread < e1 ? eb + kPullPerThread : e1;
+        const uint32_t re = (uint32_t)(ee - e0);
+        uint32_t act = 0;
+        {
+            int k = lo;
+            uint32_t nb = s_idx[k + 1];
+#pragma unroll
+            for (int q = 0; q < kPullPerThread; ++q) {
+                const uint32_t e = rb + q;
+                if (e < re) {
+                    while (e >= nb) nb = s_idx[++k + 1];
+                    if (s_v[k] != 0xFFFFFFFFu) act |= 1u << q;
+                }
+            }
+        }
+        if (act) {
+            uint32_t ids[kPullPerThread];
+            if (ee - eb == kPullPerThread) {
+                const uint4* p = reinterpret_cast<const uint4*>(adj + eb);
+#pragma unroll
+                for (int q = 0; q < kPullPerThread / 4; ++q) {
+                    const uint4 x = __ldcs(p + q);
+                    ids[4 * q] = x.x; ids[4 * q + 1] = x.y; ids[4 * q + 2] = x.z; ids[4 * q + 3] = x.w;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < kPullPerThread; ++q) ids[q] = eb + q < ee ? adj[eb + q] : 0u;
+            }
+            Acc vals[kPullPerThread];
+#pragma unroll
+            for (int q = 0; q < kPullPerThread; ++q) vals[q] = (act >> q) & 1u ? op.gather(ids[q]) : op.identity();
+            int k = lo;
+            uint32_t nb = s_idx[k + 1];
+            Acc a = op.identity();
+#pragma unroll
+            for (int q = 0; q < kPullPerThread; ++q) {
+                const uint32_t e = rb + q;
+                if (e < re) {
+                    while (e >= nb) {
+                        if (a != op.identity()) op.finish_direct(s_v[k], a);
+                        a = op.identity();
+                        ++k;
+                        nb = s_idx[k + 1];
+                    }
+                    a = op.combine(a, vals[q]);
+                }
+            }
+            fin_key = k;
+            fin = a;
+        }
+    }
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const Acc vo = __shfl_up_sync(0xffffffffu, fin, o);
+        const int ko = __shfl_up_sync(0xffffffffu, fin_key, o);
+        if (lane >= o && ko == fin_key) fin = op.combine(fin, vo);
+    }
+    const int knext = __shfl_down_sync(0xffffffffu, fin_key, 1);
+    if (fin_key != 0x7fffffff && (lane == 31 || knext != fin_key) && fin != op.identity())
+        op.finish_direct(s_v[fin_key], fin);
+}
+
+template <class Op>
+static int launch_pull_direct(eg_graph* g, const Op& op, const char* name) {
+    EngineState& s = g->eng;
+    if (s.pull_nchunks == 0) return EG_OK;
+    const uint64_t nitems = g->ncompressed - 1;
+    // a chunk holds at most one item per edge plus the zero-length sentinels of empty partitions
+    const size_t smem = 6 * ((size_t)kPullChunk + g->partitions + 3);
+    EG_CUDA(cudaFuncSetAttribute(k_pull_direct<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    Timed t(&g->prof, g->stream, name);
+    k_pull_direct<Op><<<(unsigned)s.pull_nchunks, kPullThreads, smem, g->stream>>>(
+        op, g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(), s.pull_chunk_item.as<uint32_t>(),
+        g->E, nitems, g->V);
+    EG_CHECK_LAUNCH(name);
+    return EG_OK;
+}
+
 // ---------------------------------------------------------------------------------------------
 // warp-aggregated append of activated vertices to a queue
 __device__ __forceinline__ void append_active(bool act, uint32_t w, uint32_t* q_out, uint32_t* n_out,
@@ -190,9 +312,12 @@ __device__ __forceinline__ void append_active(bool act, uint32_t w, uint32_t* q_
     uint32_t base = 0;
     if (lane == leader) base = atomicAdd(n_out, (uint32_t)__popc(mask));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (act) {
-        q_out[base + __popc(mask & ((1u << lane) - 1u))] = w;
-        if (act_edges) atomicAdd(act_edges, (unsigned long long)deg[w]);
+    if (act) q_out[base + __popc(mask & ((1u << lane) - 1u))] = w;
+    if (act_edges) {  // one add per warp: a single counter takes every warp's activations
+        unsigned long long d = act ? (unsigned long long)deg[w] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if (lane == leader) atomicAdd(act_edges, d);
     }
 }
 
@@ -235,7 +360,7 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Op op, PushArgs a) {
         uint64_t ibeg = a.ipref[it], iend = a.ipref[it + 1];
         uint32_t u = a.q[it / a.P];
         uint64_t lbase = a.off[(it % a.P) * a.stride + u];
-        uint32_t pay = op.payload(u);
+        auto pay = op.payload(u);
 #pragma unroll
         for (int q = 0; q < kPushPerThread; ++q) {
             const uint64_t e = eb + q;
