@@ -1,0 +1,131 @@
+"""Edge cases through the C ABI against the oracle: empty and one-vertex graphs, self loops and
+duplicate edges, a hub whose in-list is long enough for the segmented dense BFS step, a path deeper
+than the captured MS-BFS loop, ids out of range, and more partitions than CPBT pages."""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import lists_equal, rel_l1
+
+pytestmark = pytest.mark.gpu
+
+
+def _ref_levels(src, dst, V, root):
+    csr = oracle.build_csr(np.asarray(src, np.uint32), np.asarray(dst, np.uint32), None, V,
+                           np.array([0, V], np.uint32))
+    return csr, oracle.bfs_levels(csr["off"][0], csr["adj"], V, root)
+
+
+def test_empty_edge_list(eg_lib):
+    import endgraph_gb300 as eg
+    V = 5000
+    with eg.Graph() as g:
+        g.load_directed(np.zeros((0, 2), np.uint32), V)
+        assert g.info().E == 0
+        po, _ = g.partition()
+        assert po[0] == 0 and po[-1] == V
+        pr = g.pagerank(20, 0.85)
+        assert np.allclose(pr, 0.15)  # no in-edges: next = 1 - d every iteration
+        lv, par = g.bfs(7)
+        assert lv[7] == 0 and par[7] == 7
+        assert np.count_nonzero(lv != oracle.UNREACHED) == 1
+        levels, edges = g.msbfs(np.array([1, 2, 3], np.uint32))
+        assert edges == 0 and levels[0, 1] == 0 and np.count_nonzero(levels != 255) == 3
+
+
+def test_single_vertex_self_loop_and_duplicates(eg_lib):
+    import endgraph_gb300 as eg
+    src = np.array([0, 0, 0], np.uint32)
+    dst = np.array([0, 0, 0], np.uint32)
+    with eg.Graph() as g:
+        g.load_directed(eg.pack_edges(src, dst), 1)
+        csr, csc = g.csr(), g.csc()
+        ref = oracle.build_csr(src, dst, None, 1, np.array([0, 1], np.uint32))
+        assert lists_equal(csr["off"][0], csr["adj"], ref["off"][0], ref["adj"])
+        assert list(csc["cvert"][:1]) == [0]
+        lv, _ = g.bfs(0)
+        assert list(lv) == [0]
+        o_out, _ = oracle.degrees(src, dst, 1)
+        refc = oracle.build_csc(src, dst, None, 1, np.array([0, 1], np.uint32))
+        pr_ref = oracle.pagerank(refc["off"][0], refc["adj"], o_out, 1, 20, 0.85)
+        assert rel_l1(g.pagerank(20, 0.85), pr_ref) <= 1e-6
+
+
+@pytest.mark.parametrize("direction", [0, 2])
+def test_hub_in_list_longer_than_a_segment(eg_lib, direction):
+    """A destination with ~5000 in-edges, only one of them from the frontier and placed late in its
+    list, so the dense step must walk its head and several segments before it finds a parent."""
+    import endgraph_gb300 as eg
+    rng = np.random.default_rng(11)
+    V = 20000
+    hub, root, mid = 19999, 0, 1
+    feeders = rng.choice(np.arange(100, 19000), 5000, replace=False).astype(np.uint32)
+    src = np.concatenate([[root], feeders, [mid], rng.integers(2, 100, 3000)]).astype(np.uint32)
+    dst = np.concatenate([[mid], np.full(5000, hub), [hub], rng.integers(2, 19000, 3000)]).astype(np.uint32)
+    csr, ref = _ref_levels(src, dst, V, root)
+    with eg.Graph() as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        g.set_option(eg.EG_OPT_BFS_DIRECTION, direction)
+        lv, par = g.bfs(root)
+        assert np.array_equal(lv, ref)
+        assert lv[hub] == 2 and par[hub] == mid
+        assert oracle.bfs_check_parents(csr["off"][0], csr["adj"], V, root, lv, par) == 0
+        levels, _ = g.msbfs(np.array([root, mid], np.uint32))
+        assert np.array_equal(levels[0], np.where(ref == oracle.UNREACHED, 255, ref).astype(np.uint8))
+
+
+def test_deep_path(eg_lib):
+    """A 200-vertex chain: deeper than the 32 captured levels; 254 levels are the u8 limit of MS-BFS."""
+    import endgraph_gb300 as eg
+    n = 200
+    src = np.arange(n - 1, dtype=np.uint32)
+    dst = src + 1
+    with eg.Graph() as g:
+        g.load_directed(eg.pack_edges(src, dst), n)
+        lv, _ = g.bfs(0)
+        assert np.array_equal(lv, np.arange(n))
+        for cg in (0, 1):
+            g.set_option(eg.EG_OPT_CUDA_GRAPH, cg)
+            levels, edges = g.msbfs(np.array([0, 50], np.uint32))
+            assert np.array_equal(levels[0], np.arange(n, dtype=np.uint8))
+            assert np.array_equal(levels[1][50:], np.arange(n - 50, dtype=np.uint8))
+            assert np.all(levels[1][:50] == 255)
+            assert edges == (n - 1) + (n - 51)
+    m = 300
+    src = np.arange(m - 1, dtype=np.uint32)
+    with eg.Graph() as g:
+        g.load_directed(eg.pack_edges(src, src + 1), m)
+        with pytest.raises(eg.EndGraphError):
+            g.msbfs(np.array([0], np.uint32))
+
+
+def test_ids_out_of_range_are_rejected(eg_lib):
+    import endgraph_gb300 as eg
+    with eg.Graph() as g:
+        with pytest.raises(eg.EndGraphError):
+            g.load_directed(eg.pack_edges(np.array([0, 5], np.uint32), np.array([1, 2], np.uint32)), 5)
+        # the handle stays usable after the rejected load
+        g.load_directed(eg.pack_edges(np.array([0, 4], np.uint32), np.array([1, 2], np.uint32)), 5)
+        lv, _ = g.bfs(0)
+        assert list(lv[:2]) == [0, 1]
+
+
+def test_more_partitions_than_pages(eg_lib):
+    """P = 8 on a 5,000-vertex graph (two CPBT pages): most partitions are empty, as in the reference."""
+    import endgraph_gb300 as eg
+    rng = np.random.default_rng(2)
+    V, E = 5000, 40000
+    src = rng.integers(0, V, E).astype(np.uint32)
+    dst = rng.integers(0, V, E).astype(np.uint32)
+    o_out, _ = oracle.degrees(src, dst, V)
+    ref_po, _ = oracle.cpbt(o_out, V, 8, 1, 1, 20, True)
+    with eg.Graph(partitions=8) as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        po, _ = g.partition()
+        assert np.array_equal(po, ref_po)
+        csr, ref = _ref_levels(src, dst, V, int(src[0]))
+        lv, _ = g.bfs(int(src[0]))
+        assert np.array_equal(lv, ref)
+        refc = oracle.build_csc(src, dst, None, V, np.array([0, V], np.uint32))
+        pr_ref = oracle.pagerank(refc["off"][0], refc["adj"], o_out, V, 20, 0.85)
+        assert rel_l1(g.pagerank(20, 0.85), pr_ref) <= 1e-6
