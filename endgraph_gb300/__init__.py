@@ -104,6 +104,7 @@ SIGNATURES = {
     "eg_profile_enable": ([_vp, _i32], _i32),
     "eg_profile_reset": ([_vp], _i32),
     "eg_profile_read": ([_vp, _vp, _i32, _vp], _i32),
+    "eg_selftest_bounded_wait": ([_vp, _u32], _i32),
 }
 
 _lib = None
@@ -436,6 +437,10 @@ class Graph:
 
     def profile_reset(self):
         _check(self._L.eg_profile_reset(self.h))
+
+    def selftest_bounded_wait(self, spin_cap=1000):
+        """Status of a look-back scan whose wait is made to run out (EG_ERR_TIMEOUT expected)."""
+        return self._L.eg_selftest_bounded_wait(self.h, spin_cap)
 
     def profile_read(self):
         n = ctypes.c_int()

@@ -496,4 +496,13 @@ int eg_profile_read(eg_graph* g, eg_kernel_stat* out, int cap, int* count) {
     return EG_OK;
 }
 
+int eg_selftest_bounded_wait(eg_graph* g, uint32_t spin_cap) {
+    EG_TRY(check_graph(g, "eg_selftest_bounded_wait"));
+    if (spin_cap < 1 || spin_cap > (1u << 22)) {
+        set_error("eg_selftest_bounded_wait: spin_cap must be in 1..2^22");
+        return EG_ERR_INVALID;
+    }
+    return selftest_bounded_wait(g, spin_cap);
+}
+
 }  // extern "C"

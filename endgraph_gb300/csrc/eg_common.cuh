@@ -198,6 +198,7 @@ int cpbt_device(eg_graph* g, const uint32_t* d_deg, uint32_t V, int P, int S, ui
                 uint32_t* h_part, uint32_t* h_local);
 int cpbt_search(eg_graph* g, const uint64_t* d_w, uint32_t n, int P, int S, uint32_t* po, uint32_t* lpo);
 int check_device_error(eg_graph* g, const char* what);
+int selftest_bounded_wait(eg_graph* g, uint32_t spin_cap);
 int validate_edges(eg_graph* g, uint64_t E);
 int symmetrize_edges(eg_graph* g, uint64_t E);
 int run_pagerank(eg_graph* g, int iterations, float damping, float* out, int where);

@@ -32,7 +32,8 @@ __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
 
 template <class Load, class Epi>
 __global__ void __launch_bounds__(kScanThreads) k_scan(Load load, Epi epi, uint64_t n, uint64_t* desc,
-                                                        uint32_t* ticket, int* err, uint64_t* total_out) {
+                                                        uint32_t* ticket, int* err, uint64_t* total_out,
+                                                        uint32_t spin_cap) {
     __shared__ uint32_t s_vals[kScanTile + kScanTile / 32];
     __shared__ uint64_t s_warp[kScanThreads / 32];
     __shared__ uint64_t s_prefix;
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Load load, Epi epi, uint6
                 uint64_t d = idx >= 0 ? ld_volatile_u64(&desc[idx]) : kStInc;
                 uint32_t st = (uint32_t)(d >> 62);
                 if (__any_sync(0xffffffffu, st == 0)) {
-                    if (++spins > kLookbackSpinCap) {
+                    if (++spins > spin_cap) {
                         timed_out = true;
                         break;
                     }
@@ -136,7 +137,7 @@ int launch_scan(eg_graph* g, Load load, Epi epi, uint64_t n, uint64_t* total_out
     Timed t(&g->prof, g->stream, name);
     k_scan<<<(unsigned)tiles, kScanThreads, 0, g->stream>>>(load, epi, n, g->scan.desc.as<uint64_t>(),
                                                             g->scan.counter.as<uint32_t>(), g->err.as<int>(),
-                                                            total_out);
+                                                            total_out, kLookbackSpinCap);
     EG_CHECK_LAUNCH(name);
     return EG_OK;
 }

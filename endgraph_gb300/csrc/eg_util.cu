@@ -136,6 +136,27 @@ int scan_exclusive_u32(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* ou
     return launch_scan(g, LoadU32{in}, EpiExclusive{out}, n, out + n, "scan_buckets");
 }
 
+// The bounded look-back wait, exercised: one CTA is launched for a two-tile scan with the ticket
+// counter already at 1, so it takes tile 1 and waits for a tile-0 descriptor that nothing
+// publishes.  After spin_cap polls it raises the error flag and finishes; the caller sees
+// EG_ERR_TIMEOUT and the handle stays usable.
+int selftest_bounded_wait(eg_graph* g, uint32_t spin_cap) {
+    const uint64_t n = 2ull * kScanTile;
+    EG_TRY(g->tmp64.reserve(sizeof(uint64_t) * n + sizeof(uint32_t) * n));
+    uint64_t* out = g->tmp64.as<uint64_t>();
+    uint32_t* in = reinterpret_cast<uint32_t*>(out + n);
+    EG_TRY(g->scan.desc.reserve(2 * sizeof(uint64_t)));
+    EG_TRY(g->scan.counter.reserve(16));
+    EG_CUDA(cudaMemsetAsync(in, 0, sizeof(uint32_t) * n, g->stream));
+    EG_CUDA(cudaMemsetAsync(g->scan.desc.ptr, 0, 2 * sizeof(uint64_t), g->stream));
+    const uint32_t one = 1;
+    EG_CUDA(cudaMemcpyAsync(g->scan.counter.ptr, &one, 4, cudaMemcpyHostToDevice, g->stream));
+    k_scan<<<1, kScanThreads, 0, g->stream>>>(LoadU32{in}, EpiExclusive{out}, n, g->scan.desc.as<uint64_t>(),
+                                              g->scan.counter.as<uint32_t>(), g->err.as<int>(), nullptr, spin_cap);
+    EG_CHECK_LAUNCH("k_scan");
+    return check_device_error(g, "eg_selftest_bounded_wait");
+}
+
 // ---------------------------------------------------------------------------------------------
 // compressed incoming index (core/graph.hpp:1144-1188): one (vertex, start) per non-empty list
 // (p, v) plus a sentinel (V, partition end) per partition; cnt holds P*(V+1) counts with the

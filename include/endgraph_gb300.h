@@ -251,6 +251,13 @@ int eg_profile_reset(eg_graph* g);
 /* fills up to cap entries, returns the number of kernels via *count */
 int eg_profile_read(eg_graph* g, eg_kernel_stat* out, int cap, int* count);
 
+/* ---- failure handling, exercised without a fault ------------------------------------------- */
+/* Every device-side wait of the library is bounded (the reference instead asserts or exits,
+ * core/graph.hpp:87,227,764-771).  This call runs the decoupled look-back scan with its first tile
+ * withheld, so the wait of the second tile runs out after spin_cap polls (1 .. 2^22).  Returns
+ * EG_ERR_TIMEOUT, as any exhausted wait does, and leaves the handle and its context usable. */
+int eg_selftest_bounded_wait(eg_graph* g, uint32_t spin_cap);
+
 #ifdef __cplusplus
 }
 #endif

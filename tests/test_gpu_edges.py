@@ -129,3 +129,18 @@ def test_more_partitions_than_pages(eg_lib):
         refc = oracle.build_csc(src, dst, None, V, np.array([0, V], np.uint32))
         pr_ref = oracle.pagerank(refc["off"][0], refc["adj"], o_out, V, 20, 0.85)
         assert rel_l1(g.pagerank(20, 0.85), pr_ref) <= 1e-6
+
+
+def test_bounded_wait_runs_out_and_handle_survives(eg_lib):
+    """A look-back wait on a descriptor that nothing publishes gives up after its poll limit: the
+    call returns EG_ERR_TIMEOUT (no trap, no hang) and the same handle keeps working."""
+    import endgraph_gb300 as eg
+    src = np.array([0, 1, 2], np.uint32)
+    dst = np.array([1, 2, 3], np.uint32)
+    with eg.Graph() as g:
+        assert g.selftest_bounded_wait(0) == 1  # EG_ERR_INVALID: the poll limit must be >= 1
+        assert g.selftest_bounded_wait(1000) == 5  # EG_ERR_TIMEOUT
+        assert b"bounded device wait" in eg_lib.eg_last_error()
+        g.load_directed(eg.pack_edges(src, dst), 4)
+        lv, _ = g.bfs(0)
+        assert list(lv) == [0, 1, 2, 3]
