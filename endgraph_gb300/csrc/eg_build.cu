@@ -293,7 +293,7 @@ __global__ void k_part_edges(const uint64_t* off, uint32_t V, int P, uint64_t E,
 //      (degrees and offsets written coalesced), then the scatter into the bucket's contiguous
 //      output range through shared-memory cursors
 // =============================================================================================
-constexpr int kBucketThreads = 512;
+constexpr int kBucketThreads = 1024;
 constexpr int kBuildThreads = 1024;
 constexpr uint32_t kMaxBucketVerts = 32768;  // 128 KiB of shared-memory counters in pass C
 constexpr int kBuildUnroll = 4;

@@ -91,12 +91,17 @@ __global__ void __launch_bounds__(256) k_bu_head(BuArgs a) {
                 const uint64_t s = a.cidx[i], e = a.cidx[i + 1];
                 const uint64_t h = e - s > kBuHead ? s + kBuHead : e;
                 uint32_t par = 0xFFFFFFFFu;
-                for (uint64_t p = s; p < h; ++p) {
-                    const uint32_t u = __ldg(a.adj + p);
-                    if (bu_in_front(a, u)) {
-                        par = u;
-                        break;
-                    }
+                // four independent id loads, then four independent frontier probes per round
+                for (uint64_t p = s; p < h && par == 0xFFFFFFFFu; p += 4) {
+                    uint32_t u[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) u[q] = p + q < h ? __ldg(a.adj + p + q) : 0xFFFFFFFFu;
+                    bool hit[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) hit[q] = u[q] != 0xFFFFFFFFu && bu_in_front(a, u[q]);
+#pragma unroll
+                    for (int q = 3; q >= 0; --q)
+                        if (hit[q]) par = u[q];
                 }
                 if (par != 0xFFFFFFFFu) act = bu_claim(a, v, par);
                 else if (e > h) nsg = (uint32_t)((e - h + kBuSeg - 1) / kBuSeg);
