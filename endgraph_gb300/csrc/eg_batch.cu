@@ -88,40 +88,6 @@ struct MsBfsPushOp {
     }
 };
 
-// next frontier bitmap -> vertex queue, its length and the out-edges of the queued vertices;
-// one warp per 32 words
-__global__ void k_bm_compact(const unsigned long long* __restrict__ bm, uint64_t nwords, uint32_t* q, uint32_t* nq,
-                             unsigned long long* act_edges, const uint32_t* __restrict__ deg) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < nwords; base += stride) {
-        const uint64_t w = base + lane;
-        unsigned long long word = w < nwords ? bm[w] : 0ull;
-        const uint32_t cnt = (uint32_t)__popcll(word);
-        uint32_t incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
-        if (!tot) continue;
-        uint32_t at = 0;
-        if (lane == 31) at = atomicAdd(nq, tot);
-        at = __shfl_sync(0xffffffffu, at, 31) + incl - cnt;
-        unsigned long long d = 0;
-        while (word) {
-            const uint32_t v = (uint32_t)(w * 64 + (uint64_t)(__ffsll((long long)word) - 1));
-            word &= word - 1;
-            q[at++] = v;
-            d += deg[v];
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-        if (lane == 0 && act_edges && d) atomicAdd(act_edges, d);
-    }
-}
-
 // level bytes of the queued vertices' new bits (row v of [V][64]: 16 threads, one 4-byte word
 // each) and the OR of their words, i.e. the roots whose traversal is still running
 __global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n_dev,

@@ -1,0 +1,536 @@
+// endgraph_gb300_engine.cuh — Gemini's process_edges / process_vertices (core/graph.hpp:1376-1817
+// of the reference) for operators written as device functors, on a graph that libendgraph_gb300
+// has loaded and built (eg_load_directed / eg_load_undirected_from_directed).  Header-only host
+// and device code: include it from a .cu file compiled for sm_103a and link the library.
+//
+// The reference passes four host lambdas (sparse_signal, sparse_slot, dense_signal, dense_slot)
+// that the engine calls per vertex and per adjacency list.  Here the same four roles are device
+// member functions of one operator type, split per edge so that the engine can balance hubs and
+// leaves (rank-balanced push over the frontier's out-edges; chunked pull over the CSC):
+//
+//   struct Op {
+//     using Msg = ...;  // sparse message (any trivially copyable type)
+//     using Acc = ...;  // dense reduction (4 or 8 bytes, trivially copyable)
+//     using R   = ...;  // value summed over slots: int, unsigned, unsigned long long, float or double
+//     // sparse (push): for every vertex of the active subset; true = emit(v, msg)
+//     __device__ bool sparse_signal(uint32_t v, Msg& msg) const;
+//     // for every out-edge (v, dst, w) of an emitting vertex (w = 0 on unweighted graphs)
+//     __device__ R sparse_slot(uint32_t v, const Msg& msg, uint32_t dst, float w) const;
+//     // dense (pull): destinations to reduce into (the reference's dense_signal returns early for
+//     // the others)
+//     __device__ bool dense_active(uint32_t dst) const;
+//     __device__ Acc dense_identity() const;
+//     // contribution of in-edge (src, dst, w); the identity contributes nothing
+//     __device__ Acc dense_signal(uint32_t src, float w) const;
+//     __device__ Acc dense_combine(Acc a, Acc b) const;
+//     // once per active destination with in-edges, with the reduction over all of its in-edges
+//     // (the identity when none contributed)
+//     __device__ R dense_slot(uint32_t dst, Acc acc) const;
+//   };
+//
+// Differences from the reference that an operator must respect: dense_slot sees the complete
+// reduction of a destination once (the reference may deliver one partial message per partition);
+// slots run concurrently and must use atomics for shared state, as the reference's slots do
+// (core/atomic.hpp); a destination's contributions combine in any order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "endgraph_gb300.h"
+#include "endgraph_gb300_kernels.cuh"
+
+namespace eg {
+namespace engine {
+
+class Error : public std::runtime_error {
+   public:
+    int status;
+    Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+inline void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw Error(EG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+inline void check_eg(int st, const char* what) {
+    if (st != EG_OK) throw Error(st, std::string(what) + ": " + eg_last_error());
+}
+
+// VertexSubset (core/bitmap.hpp:23-68) in device memory: bit v of words[v / 64]
+struct Subset {
+    unsigned long long* words = nullptr;
+    uint32_t V = 0;
+    __device__ __forceinline__ bool get_bit(uint32_t v) const { return (__ldcg(words + (v >> 6)) >> (v & 63)) & 1ull; }
+    __device__ __forceinline__ void set_bit(uint32_t v) const { atomicOr(words + (v >> 6), 1ull << (v & 63)); }
+    size_t nwords() const { return (size_t)V / 64 + 1; }
+};
+
+enum class Mode { Auto, Sparse, Dense };
+
+namespace detail {
+
+template <class T>
+__device__ __forceinline__ auto to_bits(T v) {
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "dense accumulators are 4 or 8 bytes");
+    using U = std::conditional_t<sizeof(T) == 4, unsigned int, unsigned long long>;
+    U u;
+    memcpy(&u, &v, sizeof(T));
+    return u;
+}
+template <class T, class U>
+__device__ __forceinline__ T from_bits(U u) {
+    T v;
+    memcpy(&v, &u, sizeof(T));
+    return v;
+}
+// *p = comb(*p, v) atomically (shared or global memory)
+template <class T, class C>
+__device__ __forceinline__ void atomic_combine(T* p, T v, const C& comb) {
+    using U = decltype(to_bits(v));
+    U* a = reinterpret_cast<U*>(p);
+    U old = *reinterpret_cast<volatile U*>(a);
+    while (true) {
+        const U nw = to_bits(comb(from_bits<T>(old), v));
+        if (nw == old) return;
+        const U seen = atomicCAS(a, old, nw);
+        if (seen == old) return;
+        old = seen;
+    }
+}
+template <class R>
+__device__ __forceinline__ void warp_add_out(R r, R* out) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if ((threadIdx.x & 31) == 0 && r != R(0)) atomicAdd(out, r);
+}
+
+template <class Op>
+struct PushAdapter {
+    using Msg = typename Op::Msg;
+    using Value = typename Op::R;
+    Op op;
+    const Msg* msg;
+    const float* w;
+    Value* out;
+    __device__ Msg payload(uint32_t u) const { return msg[u]; }
+    __device__ bool relax(uint32_t u, const Msg& m, uint32_t dst, uint64_t pos, Value& acc) const {
+        acc += op.sparse_slot(u, m, dst, w ? w[pos] : 0.f);
+        return false;
+    }
+    __device__ void reduce_out(Value v) const {
+        if (v != Value(0)) atomicAdd(out, v);
+    }
+};
+
+template <class Op>
+struct PullAdapter {
+    using Acc = typename Op::Acc;
+    using R = typename Op::R;
+    static constexpr bool kFilter = true;
+    Op op;
+    const float* w;
+    Acc* partial;  // [V] combined partial reductions of destinations split across chunks
+    R* out;
+    int single;    // one partition: an item wholly inside a chunk is the whole destination
+    __device__ bool stopped() const { return false; }
+    __device__ bool item_active(uint32_t v) const { return op.dense_active(v); }
+    __device__ Acc identity() const { return op.dense_identity(); }
+    __device__ Acc gather(uint32_t u, uint64_t pos) const { return op.dense_signal(u, w ? w[pos] : 0.f); }
+    __device__ Acc combine(Acc a, Acc b) const { return op.dense_combine(a, b); }
+    __device__ void smem_add(Acc* slot, Acc v) const {
+        if (to_bits(v) != to_bits(identity()))
+            atomic_combine(slot, v, [this](Acc x, Acc y) { return op.dense_combine(x, y); });
+    }
+    __device__ void finish(bool ok, uint32_t v, Acc a, bool whole) const {
+        R r = R(0);
+        if (ok && op.dense_active(v)) {
+            if (whole && single) {
+                r = op.dense_slot(v, a);
+            } else if (to_bits(a) != to_bits(identity())) {
+                atomic_combine(partial + v, a, [this](Acc x, Acc y) { return op.dense_combine(x, y); });
+            }
+        }
+        warp_add_out(r, out);
+    }
+};
+
+template <class Op>
+__global__ void k_sparse_signal(Op op, const uint32_t* __restrict__ q, const uint32_t* nq, typename Op::Msg* msg,
+                                uint32_t* q_out, uint32_t* n_out) {
+    const uint32_t n = __ldcg(nq);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint64_t i = base + threadIdx.x;
+        bool emit = false;
+        uint32_t v = 0;
+        if (i < n) {
+            v = q[i];
+            typename Op::Msg m;
+            emit = op.sparse_signal(v, m);
+            if (emit) msg[v] = m;
+        }
+        append_active(emit, v, q_out, n_out, nullptr, nullptr);
+    }
+}
+
+template <class Op>
+__global__ void k_fill_acc(typename Op::Acc* p, uint64_t n, Op op) {
+    const typename Op::Acc id = op.dense_identity();
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = id;
+}
+
+// destinations whose reduction was combined in `partial`: the split list (one partition) or every
+// vertex with in-edges (several partitions)
+template <class Op>
+__global__ void k_dense_finish(Op op, const uint32_t* __restrict__ split, const uint32_t* __restrict__ cvert,
+                               uint64_t nsplit, const uint32_t* __restrict__ indeg, uint32_t V,
+                               typename Op::Acc* partial, typename Op::R* out) {
+    using R = typename Op::R;
+    const uint64_t n = split ? nsplit : V;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint64_t i = base + threadIdx.x;
+        R r = R(0);
+        if (i < n) {
+            const uint32_t v = split ? cvert[split[i]] : (uint32_t)i;
+            if (v < V && (split || indeg[v] > 0) && op.dense_active(v)) {
+                const typename Op::Acc a = partial[v];
+                partial[v] = op.dense_identity();
+                r = op.dense_slot(v, a);
+            }
+        }
+        warp_add_out(r, out);
+    }
+}
+
+template <class R, class F>
+__global__ void k_vertices(F f, const unsigned long long* __restrict__ words, uint64_t nwords, uint32_t V, R* out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nwords; base += stride) {
+        const uint64_t w = base + threadIdx.x;
+        R r = R(0);
+        if (w < nwords) {
+            unsigned long long word = words[w];
+            while (word) {
+                const uint32_t v = (uint32_t)(w * 64 + (uint64_t)(__ffsll((long long)word) - 1));
+                word &= word - 1;
+                if (v < V) r += f(v);
+            }
+        }
+        warp_add_out(r, out);
+    }
+}
+
+static __global__ void k_fill_words(unsigned long long* words, uint64_t nwords, uint32_t V) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords; w += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t lo = w * 64;
+        unsigned long long x = 0;
+        if (lo + 64 <= V) x = ~0ull;
+        else if (lo < V) x = (1ull << (V - lo)) - 1ull;
+        words[w] = x;
+    }
+}
+
+}  // namespace detail
+
+// One engine per built graph.  All work is ordered on the graph handle's stream; the results of
+// process_edges / process_vertices are returned to the host (one synchronisation per call).
+class Engine {
+   public:
+    explicit Engine(eg_graph* g) : g_(g) {
+        eg_info info;
+        check_eg(eg_get_info(g, &info), "eg_get_info");
+        if (!info.built_csr || !info.built_csc) throw Error(EG_ERR_STATE, "Engine: build CSR and CSC first");
+        V_ = info.V;
+        E_ = info.E;
+        P_ = (int)info.partitions;
+        nitems_ = info.ncompressed - 1;
+        check_eg(eg_get_csr(g, &csr_), "eg_get_csr");
+        check_eg(eg_get_csc(g, &csc_), "eg_get_csc");
+        stream_ = (cudaStream_t)eg_stream(g);
+        int dev = 0;
+        check(cudaGetDevice(&dev), "cudaGetDevice");
+        check(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+        outdeg_ = alloc<uint32_t>(V_);
+        indeg_ = alloc<uint32_t>(V_);
+        check_eg(eg_get_degrees(g, outdeg_, indeg_, EG_DEVICE), "eg_get_degrees");
+        counters_ = alloc<unsigned long long>(8);
+        q0_ = alloc<uint32_t>((size_t)V_ + 1);
+        q1_ = alloc<uint32_t>((size_t)V_ + 1);
+        ipref_ = alloc<uint64_t>((size_t)V_ * P_ + 2);
+        push_chunk_ = alloc<uint32_t>(E_ / kPushChunk + 4);
+        scan_desc_ = alloc<uint64_t>(((size_t)V_ * P_ + kScanTile) / kScanTile + 1);
+        // pull chunks: first compressed entry per 4096-edge chunk and the entries crossing chunks
+        nchunks_ = (E_ + kPullChunk - 1) / kPullChunk;
+        pull_chunk_ = alloc<uint32_t>(nchunks_ + 2);
+        split_ = alloc<uint32_t>(nchunks_ + 2);
+        check(cudaMemsetAsync(counters_, 0, 64, stream_), "cudaMemsetAsync");
+        k_pull_chunks<<<grid(nitems_), 256, 0, stream_>>>(csc_.cidx, csc_.cvert, nitems_, nchunks_, pull_chunk_, split_,
+                                                         counters_);
+        check(cudaGetLastError(), "k_pull_chunks");
+        check(cudaMemcpyAsync(&nsplit_, counters_, 8, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    }
+    ~Engine() {
+        for (void* p : {(void*)outdeg_, (void*)indeg_, (void*)counters_, (void*)q0_, (void*)q1_, (void*)ipref_,
+                        (void*)push_chunk_, (void*)scan_desc_, (void*)pull_chunk_, (void*)split_, msg_, partial_})
+            if (p) cudaFree(p);
+    }
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    uint32_t vertices() const { return V_; }
+    uint64_t edges() const { return E_; }
+    cudaStream_t stream() const { return stream_; }
+    const uint32_t* out_degree() const { return outdeg_; }  // device
+    const uint32_t* in_degree() const { return indeg_; }    // device
+    bool last_was_dense() const { return last_dense_; }
+    uint64_t last_active_edges() const { return last_active_edges_; }
+
+    // vertex arrays and subsets in device memory (alloc_vertex_array / alloc_vertex_subset)
+    template <class T>
+    T* alloc_vertex_array() {
+        return alloc<T>(V_);
+    }
+    template <class T>
+    void fill_vertex_array(T* a, T value) {
+        std::vector<T> h((size_t)V_, value);
+        check(cudaMemcpyAsync(a, h.data(), sizeof(T) * (size_t)V_, cudaMemcpyHostToDevice, stream_), "fill");
+        check(cudaStreamSynchronize(stream_), "fill");
+    }
+    void free(void* p) { cudaFree(p); }
+    Subset alloc_subset() {
+        Subset s;
+        s.V = V_;
+        s.words = alloc<unsigned long long>(s.nwords());
+        clear(s);
+        return s;
+    }
+    void free_subset(Subset& s) {
+        cudaFree(s.words);
+        s.words = nullptr;
+    }
+    void clear(const Subset& s) { check(cudaMemsetAsync(s.words, 0, 8 * s.nwords(), stream_), "clear"); }
+    void fill(const Subset& s) {
+        detail::k_fill_words<<<grid(s.nwords()), 256, 0, stream_>>>(s.words, s.nwords(), V_);
+        check(cudaGetLastError(), "k_fill_words");
+    }
+    void set_bit(const Subset& s, uint32_t v) {  // host-side, stream-ordered
+        if (v >= V_) throw Error(EG_ERR_INVALID, "set_bit: vertex out of range");
+        unsigned long long word = 0;
+        check(cudaMemcpyAsync(&word, s.words + (v >> 6), 8, cudaMemcpyDeviceToHost, stream_), "set_bit");
+        check(cudaStreamSynchronize(stream_), "set_bit");
+        word |= 1ull << (v & 63);
+        check(cudaMemcpyAsync(s.words + (v >> 6), &word, 8, cudaMemcpyHostToDevice, stream_), "set_bit");
+        check(cudaStreamSynchronize(stream_), "set_bit");
+    }
+
+    // sum of f(v) over the vertices of `active` (core/graph.hpp:1377-1441); f is a device functor
+    template <class R, class F>
+    R process_vertices(const F& f, const Subset& active) {
+        R* out = reinterpret_cast<R*>(counters_ + 6);
+        check(cudaMemsetAsync(out, 0, sizeof(R), stream_), "cudaMemsetAsync");
+        detail::k_vertices<R, F><<<grid(active.nwords()), 256, 0, stream_>>>(f, active.words, active.nwords(), V_, out);
+        check(cudaGetLastError(), "k_vertices");
+        R h{};
+        check(cudaMemcpyAsync(&h, out, sizeof(R), cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        return h;
+    }
+
+    // core/graph.hpp:1473-1817.  Auto takes the sparse (push) path iff the active vertices' out-edges
+    // are fewer than E / dense_divisor (the reference's E / 20, :1484-1491); the dense path does not
+    // read `active` (an operator's dense_signal consults it, as the reference's dense_signal does).
+    template <class Op>
+    typename Op::R process_edges(const Op& op, const Subset& active, Mode mode = Mode::Auto, int dense_divisor = 20) {
+        using R = typename Op::R;
+        static_assert(std::is_trivially_copyable<Op>::value, "operators are passed to kernels by value");
+        R* out = reinterpret_cast<R*>(counters_ + 6);
+        check(cudaMemsetAsync(out, 0, sizeof(R), stream_), "cudaMemsetAsync");
+        uint32_t* d_n = reinterpret_cast<uint32_t*>(counters_ + 2);
+        unsigned long long* d_act = counters_ + 3;
+        bool dense = mode == Mode::Dense;
+        uint32_t n_active = 0;
+        if (mode != Mode::Dense) {
+            check(cudaMemsetAsync(counters_ + 2, 0, 16, stream_), "cudaMemsetAsync");
+            k_bm_compact<<<grid(active.nwords()), 256, 0, stream_>>>(active.words, active.nwords(), q0_, d_n, d_act,
+                                                                     outdeg_);
+            check(cudaGetLastError(), "k_bm_compact");
+            struct {
+                uint32_t n, pad;
+                unsigned long long act;
+            } h;
+            check(cudaMemcpyAsync(&h, counters_ + 2, 16, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+            check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+            n_active = h.n;
+            last_active_edges_ = h.act;
+            dense = mode == Mode::Auto && h.act >= E_ / (uint64_t)std::max(dense_divisor, 1);
+        }
+        last_dense_ = dense;
+        if (dense) run_dense(op, out);
+        else if (n_active) run_sparse(op, n_active, out);
+        R h{};
+        check(cudaMemcpyAsync(&h, out, sizeof(R), cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        return h;
+    }
+
+   private:
+    template <class T>
+    T* alloc(size_t n) {
+        void* p = nullptr;
+        check(cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)), "cudaMalloc");
+        return static_cast<T*>(p);
+    }
+    unsigned grid(uint64_t n, unsigned block = 256) const {
+        uint64_t b = (n + block - 1) / block;
+        b = std::max<uint64_t>(b, 1);
+        return (unsigned)std::min<uint64_t>(b, (uint64_t)num_sms_ * 16u);
+    }
+
+    template <class Op>
+    void run_sparse(const Op& op, uint32_t n_active, typename Op::R* out) {
+        using Msg = typename Op::Msg;
+        if (msg_bytes_ < sizeof(Msg) * (size_t)V_) {
+            if (msg_) cudaFree(msg_);
+            msg_ = nullptr;
+            check(cudaMalloc(&msg_, sizeof(Msg) * (size_t)V_), "cudaMalloc");
+            msg_bytes_ = sizeof(Msg) * (size_t)V_;
+        }
+        Msg* msg = static_cast<Msg*>(msg_);
+        uint32_t* d_n = reinterpret_cast<uint32_t*>(counters_ + 2);
+        uint32_t* d_emit = reinterpret_cast<uint32_t*>(counters_ + 4);
+        check(cudaMemsetAsync(d_emit, 0, 4, stream_), "cudaMemsetAsync");
+        detail::k_sparse_signal<Op><<<grid(n_active), 256, 0, stream_>>>(op, q0_, d_n, msg, q1_, d_emit);
+        check(cudaGetLastError(), "k_sparse_signal");
+        uint32_t n_emit = 0;
+        check(cudaMemcpyAsync(&n_emit, d_emit, 4, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        if (!n_emit) return;
+        // ranks of the emitters' out-edges (every partition's list of every emitter)
+        const uint64_t nitems = (uint64_t)n_emit * P_;
+        const uint64_t tiles = std::max<uint64_t>((nitems + kScanTile - 1) / kScanTile, 1);
+        check(cudaMemsetAsync(scan_desc_, 0, 8 * tiles, stream_), "cudaMemsetAsync");
+        check(cudaMemsetAsync(counters_ + 5, 0, 8, stream_), "cudaMemsetAsync");  // ticket + error flag
+        uint32_t* ticket = reinterpret_cast<uint32_t*>(counters_ + 5);
+        int* err = reinterpret_cast<int*>(ticket + 1);
+        LoadItemLen ld{q1_, P_, (uint64_t)V_ + 1, csr_.off};
+        EpiItemRank ep{ipref_, push_chunk_};
+        k_scan<<<(unsigned)tiles, kScanThreads, 0, stream_>>>(ld, ep, nitems, scan_desc_, ticket, err, ipref_ + nitems,
+                                                             kLookbackSpinCap);
+        check(cudaGetLastError(), "k_scan");
+        PushArgs a;
+        a.q = q1_;
+        a.nitems = nitems;
+        a.P = P_;
+        a.stride = (uint64_t)V_ + 1;
+        a.off = csr_.off;
+        a.adj = csr_.adj;
+        a.w = csr_.w;
+        a.ipref = ipref_;
+        a.chunk_item = push_chunk_;
+        a.q_out = nullptr;
+        a.n_out = nullptr;
+        a.act_edges = nullptr;
+        a.deg = nullptr;
+        detail::PushAdapter<Op> pa{op, msg, csr_.w, out};
+        k_push<detail::PushAdapter<Op>><<<(unsigned)num_sms_ * 8u, kPushThreads, 0, stream_>>>(pa, a);
+        check(cudaGetLastError(), "k_push");
+        int h_err = 0;
+        check(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        if (h_err) throw Error(EG_ERR_TIMEOUT, "process_edges: a bounded device wait gave up");
+    }
+
+    template <class Op>
+    void run_dense(const Op& op, typename Op::R* out) {
+        using Acc = typename Op::Acc;
+        if (nchunks_ == 0) return;
+        // partial reductions start at the operator's identity
+        const typename Op::Acc id = host_identity(op);
+        unsigned long long id_bits = 0;
+        memcpy(&id_bits, &id, sizeof(Acc));
+        if (partial_bytes_ < sizeof(Acc) * (size_t)V_ || partial_size_ != sizeof(Acc) || partial_id_ != id_bits) {
+            if (partial_bytes_ < sizeof(Acc) * (size_t)V_) {
+                if (partial_) cudaFree(partial_);
+                partial_ = nullptr;
+                check(cudaMalloc(&partial_, sizeof(Acc) * (size_t)V_), "cudaMalloc");
+                partial_bytes_ = sizeof(Acc) * (size_t)V_;
+            }
+            detail::k_fill_acc<Op><<<grid(V_), 256, 0, stream_>>>(static_cast<Acc*>(partial_), V_, op);
+            check(cudaGetLastError(), "k_fill_acc");
+            partial_size_ = sizeof(Acc);
+            partial_id_ = id_bits;
+        }
+        detail::PullAdapter<Op> pa{op, csc_.w, static_cast<Acc*>(partial_), out, P_ == 1 ? 1 : 0};
+        using K = detail::PullAdapter<Op>;
+        const int cap = (int)kPullChunk + P_ + 2;
+        const size_t smem = sizeof(uint32_t) * (cap + 1) + sizeof(Acc) * cap + cap;
+        check(cudaFuncSetAttribute(k_pull<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem");
+        int per_sm = 0;
+        check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<K>, kPullThreads, smem), "occupancy");
+        const unsigned g = (unsigned)std::min<uint64_t>(nchunks_, (uint64_t)num_sms_ * (uint64_t)std::max(per_sm, 1));
+        k_pull<K><<<g, kPullThreads, smem, stream_>>>(pa, csc_.adj, csc_.cidx, csc_.cvert, pull_chunk_, E_, nitems_,
+                                                     nchunks_, V_, cap);
+        check(cudaGetLastError(), "k_pull");
+        const uint64_t n = P_ == 1 ? nsplit_ : V_;
+        if (n)
+            detail::k_dense_finish<Op><<<grid(n), 256, 0, stream_>>>(op, P_ == 1 ? split_ : nullptr, csc_.cvert,
+                                                                    nsplit_, indeg_, V_, static_cast<Acc*>(partial_),
+                                                                    out);
+        check(cudaGetLastError(), "k_dense_finish");
+    }
+
+    // the identity is a device function; evaluate it once on the device
+    template <class Op>
+    typename Op::Acc host_identity(const Op& op) {
+        using Acc = typename Op::Acc;
+        Acc* d = reinterpret_cast<Acc*>(counters_ + 7);
+        detail::k_fill_acc<Op><<<1, 1, 0, stream_>>>(d, 1, op);
+        check(cudaGetLastError(), "k_fill_acc");
+        Acc h;
+        check(cudaMemcpyAsync(&h, d, sizeof(Acc), cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        return h;
+    }
+
+    eg_graph* g_;
+    uint32_t V_ = 0;
+    uint64_t E_ = 0;
+    int P_ = 1;
+    uint64_t nitems_ = 0;
+    eg_csr_view csr_{};
+    eg_csc_view csc_{};
+    cudaStream_t stream_ = nullptr;
+    int num_sms_ = 152;
+    uint32_t* outdeg_ = nullptr;
+    uint32_t* indeg_ = nullptr;
+    unsigned long long* counters_ = nullptr;  // [2..3] queue length + active edges, [4] emitters, [5] scan ticket/error, [6] result, [7] identity
+    uint32_t* q0_ = nullptr;
+    uint32_t* q1_ = nullptr;
+    uint64_t* ipref_ = nullptr;
+    uint32_t* push_chunk_ = nullptr;
+    uint64_t* scan_desc_ = nullptr;
+    uint64_t nchunks_ = 0;
+    uint32_t* pull_chunk_ = nullptr;
+    uint32_t* split_ = nullptr;
+    unsigned long long nsplit_ = 0;
+    void* msg_ = nullptr;
+    size_t msg_bytes_ = 0;
+    void* partial_ = nullptr;
+    size_t partial_bytes_ = 0, partial_size_ = 0;
+    unsigned long long partial_id_ = 0;
+    bool last_dense_ = false;
+    uint64_t last_active_edges_ = 0;
+};
+
+}  // namespace engine
+}  // namespace eg

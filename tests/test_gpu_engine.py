@@ -1,0 +1,95 @@
+"""The device operator API (include/endgraph_gb300_engine.cuh): the four reference toolkits written
+as signal/slot device functors (tests/engine/engine_toolkits.cu) against the oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import rel_l1, rmat_graph
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "engine", "engine_toolkits.cu")
+LIBDIR = os.path.join(ROOT, "endgraph_gb300")
+
+
+def _compile(out):
+    cmd = ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
+           "-I", os.path.join(ROOT, "include"), SRC, "-o", out, "-L", LIBDIR, "-lendgraph_gb300",
+           "-Xlinker", f"-rpath={LIBDIR}"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+def test_engine_header_compiles_for_sm103a(tmp_path):
+    from endgraph_gb300 import build
+    build.build()
+    _compile(str(tmp_path / "engine_toolkits"))
+
+
+@pytest.fixture(scope="module")
+def engine_exe(tmp_path_factory):
+    from endgraph_gb300 import build
+    build.build()
+    return _compile(str(tmp_path_factory.mktemp("engine") / "engine_toolkits"))
+
+
+def _run(exe, tmp_path, algo, rec, V, arg):
+    f = tmp_path / f"{algo}.bin"
+    rec.tofile(f)
+    out = tmp_path / f"{algo}.out"
+    r = subprocess.run([exe, algo, str(f), str(V), str(arg), str(out)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return out, r.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("V,E,seed", [(1 << 14, 1 << 18, 5), (100_000, 600_000, 6)])
+def test_engine_pagerank_fp64(engine_exe, tmp_path, V, E, seed):
+    import endgraph_gb300 as eg
+    src, dst, _ = rmat_graph(V, E, seed)
+    out, _ = _run(engine_exe, tmp_path, "pagerank", eg.pack_edges(src, dst), V, 20)
+    pr = np.fromfile(out, np.float64)
+    o_out, _ = oracle.degrees(src, dst, V)
+    csc = oracle.build_csc(src, dst, None, V, np.array([0, V], np.uint32))
+    ref = oracle.pagerank(csc["off"][0], csc["adj"], o_out, V, 20, 0.85)
+    assert rel_l1(pr, ref) <= 1e-12  # both FP64; only the summation order differs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("V,E,seed", [(1 << 14, 1 << 18, 7), (1 << 16, 1 << 20, 8)])
+def test_engine_bfs(engine_exe, tmp_path, V, E, seed):
+    import endgraph_gb300 as eg
+    src, dst, _ = rmat_graph(V, E, seed)
+    root = int(src[0])
+    out, log = _run(engine_exe, tmp_path, "bfs", eg.pack_edges(src, dst), V, root)
+    a = np.fromfile(out, np.uint32)
+    lv, par = a[:V], a[V:]
+    csr = oracle.build_csr(src, dst, None, V, np.array([0, V], np.uint32))
+    assert np.array_equal(lv, oracle.bfs_levels(csr["off"][0], csr["adj"], V, root))
+    assert oracle.bfs_check_parents(csr["off"][0], csr["adj"], V, root, lv, par) == 0
+    assert '"dense_steps": 0' not in log  # the E/20 switch took the pull path at least once
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("V,E,seed", [(1 << 14, 1 << 17, 9), (100_000, 300_000, 10)])
+def test_engine_cc(engine_exe, tmp_path, V, E, seed):
+    import endgraph_gb300 as eg
+    src, dst, _ = rmat_graph(V, E, seed)
+    out, _ = _run(engine_exe, tmp_path, "cc", eg.pack_edges(src, dst), V, 0)
+    assert np.array_equal(np.fromfile(out, np.uint32), oracle.cc_labels(src, dst, V))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("V,E,seed", [(1 << 14, 1 << 17, 11), (50_000, 400_000, 12)])
+def test_engine_sssp(engine_exe, tmp_path, V, E, seed):
+    import endgraph_gb300 as eg
+    src, dst, w = rmat_graph(V, E, seed, weights=(0.0, 1.0))
+    root = int(src[0])
+    out, _ = _run(engine_exe, tmp_path, "sssp", eg.pack_edges(src, dst, w), V, root)
+    d = np.fromfile(out, np.float32)
+    csr = oracle.build_csr(src, dst, w, V, np.array([0, V], np.uint32))
+    ref = oracle.sssp(csr["off"][0], csr["adj"], csr["w"], V, root)
+    assert np.array_equal(d.view(np.uint32), ref.view(np.uint32))
