@@ -48,6 +48,8 @@ def parse_args():
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--ppr-scale", type=int, default=22)
     p.add_argument("--batch-graphs", type=int, default=1024)
+    p.add_argument("--no-power-law", action="store_true",
+                   help="skip the 41.6 M-vertex / 1.47 B-edge CC + SSSP section")
     return p.parse_args()
 
 
@@ -326,6 +328,85 @@ def run_graph_batch(args, dev):
     return out
 
 
+def run_power_law(args, dev):
+    """Twitter-2010-sized power-law graph (seeded R-MAT stand-in with 41,652,230 vertices and
+    1,468,365,182 edges, U[0,1) float weights): a weighted build, SSSP from one root, and CC on the
+    symmetrised graph (2.94 B edges).  Both results are checked at full size through properties
+    that hold only for the exact answer: no edge can still relax a distance and every reached
+    vertex's distance is attained by one in-edge (float adds, bit for bit); labels are equal across
+    every edge, never above the vertex id, and fixed points of the label map."""
+    import numpy as np
+    import torch
+
+    import endgraph_gb300 as eg
+    V, E = 41_652_230, 1_468_365_182
+    rec = torch.empty((E, 3), dtype=torch.int32, device=dev)
+    eg.generate_rmat(rec, V, E, args.seed + 21, A, B, C, permute=True, weights=(0.0, 1.0))
+    out = {"V": V, "E": E}
+    chunk = 1 << 27
+
+    with eg.Graph(eta=1, device=dev.index or 0) as g:
+        s = torch.cuda.ExternalStream(g.stream, device=dev)
+        g.load_directed(rec, V)
+        t_b, _ = _timed(s, lambda: g.load_directed(rec, V))
+        out["weighted_build_ms"] = round(t_b, 3)
+        out["weighted_build_medges_s"] = round(E / t_b / 1e3, 1)
+        outd, _ = g.degrees()
+        out["max_out_degree"] = int(outd.max())
+        rng = np.random.default_rng(args.seed + 22)
+        cand = rng.integers(0, V, 4096)
+        root = int(cand[outd[cand] > 0][0])
+        dist = torch.empty(V, dtype=torch.float32, device=dev)
+        g.sssp(root, dist)
+        t_s, _ = _timed(s, lambda: g.sssp(root, dist))
+        run = g.last_run()
+        out["sssp_ms"] = round(t_s, 3)
+        out["sssp_iterations"] = run["iterations"]
+        out["sssp_edges_relaxed"] = run["edges"]
+        out["sssp_gteps"] = round(run["edges"] / t_s / 1e6, 2)
+    torch.cuda.empty_cache()
+    best = torch.full((V,), float("inf"), dtype=torch.float32, device=dev)
+    slack_ok = True
+    for e0 in range(0, E, chunk):
+        r = rec[e0:e0 + chunk]
+        u, v = r[:, 0].long(), r[:, 1].long()
+        relax = dist[u] + r[:, 2].contiguous().view(torch.float32)
+        slack_ok &= bool((relax >= dist[v]).all())
+        best.scatter_reduce_(0, v, relax, reduce="amin")
+    reached = dist < 1e9
+    reached[root] = False
+    out["sssp_reached"] = int(reached.sum()) + 1
+    out["sssp_check"] = bool(slack_ok and bool((best[reached] == dist[reached]).all()) and float(dist[root]) == 0.0)
+    del best, dist
+    und = rec[:, :2].contiguous()
+    del rec
+    torch.cuda.empty_cache()
+
+    with eg.Graph(eta=1, device=dev.index or 0) as g:
+        s = torch.cuda.ExternalStream(g.stream, device=dev)
+        g.load_undirected_from_directed(und, V)
+        t_b, _ = _timed(s, lambda: g.load_undirected_from_directed(und, V))
+        out["undirected_build_ms"] = round(t_b, 3)
+        out["undirected_build_medges_s"] = round(2 * E / t_b / 1e3, 1)
+        label = torch.empty(V, dtype=torch.int32, device=dev)
+        g.cc(label)
+        t_c, _ = _timed(s, lambda: g.cc(label))
+        run = g.last_run()
+        out["cc_ms"] = round(t_c, 3)
+        out["cc_iterations"] = run["iterations"]
+        out["cc_push_pull"] = [run["push"], run["pull"]]
+    lab = label.long()
+    ok = bool((lab <= torch.arange(V, device=dev)).all()) and bool((lab[lab] == lab).all())
+    for e0 in range(0, E, chunk):
+        r = und[e0:e0 + chunk]
+        ok &= bool((lab[r[:, 0].long()] == lab[r[:, 1].long()]).all())
+    out["cc_components"] = int((lab == torch.arange(V, device=dev)).sum())
+    out["cc_check"] = ok
+    del und, lab, label
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -457,6 +538,12 @@ def run_ours(args, world, rank, local):
         del edges
         torch.cuda.empty_cache()
         batched["graph_batch"] = run_graph_batch(args, dev)
+    if batched is not None and not args.no_power_law:
+        if args.batch_graphs <= 0:
+            g.close()
+            del edges
+            torch.cuda.empty_cache()
+        batched["power_law"] = run_power_law(args, dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
