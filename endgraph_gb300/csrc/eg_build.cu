@@ -383,13 +383,15 @@ __device__ uint32_t block_exclusive_scan(uint32_t* s, uint32_t n, uint32_t* s_wa
     return total;
 }
 
-// B: tiles of kScatterPer x 1024 edges are counting-sorted by bucket in shared memory and then
+// B: tiles of scatter_per(REC) x 1024 edges are counting-sorted by bucket in shared memory and then
 // stored in that order, so consecutive threads store consecutive addresses of a bucket's run
 // (whole sectors instead of one partial sector per record).  The block's running base per bucket
 // starts at its exclusive (bucket, block) offset from the scan of pass A.
 constexpr int kScatterThreads = 1024;
-constexpr int kScatterPer = 8;
-constexpr int kScatterTile = kScatterThreads * kScatterPer;
+// 16 records per thread for 8-byte records (128 KiB tile: longer runs per bucket, fewer partial
+// sectors), 8 for 12-byte records so that the tile and the bucket tables still fit 200 KiB
+__host__ __device__ constexpr int scatter_per(int rec) { return rec == 8 ? 16 : 8; }
+__host__ __device__ constexpr int scatter_tile(int rec) { return kScatterThreads * scatter_per(rec); }
 
 template <int REC>
 __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_t* __restrict__ edges, uint64_t E,
@@ -400,16 +402,17 @@ __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_
     extern __shared__ __align__(16) unsigned char s_raw[];
     unsigned long long* s_base = reinterpret_cast<unsigned long long*>(s_raw);  // [2][nb]
     uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_base + 2 * nb);            // [nb]
-    uint32_t* s_stage = s_cnt + nb;                                               // [tile][W]
+    uint32_t* s_stage = reinterpret_cast<uint32_t*>(s_raw + align16(20ull * nb));  // [tile][W]
     __shared__ uint32_t s_warp[32];
     for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_base[i] = excl[(uint64_t)i * nblk + blockIdx.x];
     const uint64_t e0 = blockIdx.x * chunk;
     const uint64_t e1 = e0 + chunk < E ? e0 + chunk : E;
-    for (uint64_t t0 = e0; t0 < e1; t0 += kScatterTile) {
-        uint32_t rec[kScatterPer][W];
-        bool valid[kScatterPer];
+    constexpr int kPer = scatter_per(REC);
+    for (uint64_t t0 = e0; t0 < e1; t0 += scatter_tile(REC)) {
+        uint32_t rec[kPer][W];
+        bool valid[kPer];
 #pragma unroll
-        for (int j = 0; j < kScatterPer; ++j) {
+        for (int j = 0; j < kPer; ++j) {
             const uint64_t e = t0 + (uint64_t)j * blockDim.x + threadIdx.x;
             valid[j] = e < e1;
             if (valid[j]) {
@@ -422,19 +425,23 @@ __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_
         for (int half = 0; half < 2; ++half) {
             for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) s_cnt[i] = 0;
             __syncthreads();
-            uint32_t rank[kScatterPer];
+            uint32_t rank[kPer];
 #pragma unroll
-            for (int j = 0; j < kScatterPer; ++j)
+            for (int j = 0; j < kPer; ++j)
                 rank[j] = valid[j] ? atomicAdd(&s_cnt[rec[j][half] >> shift], 1u) : 0u;
             __syncthreads();
             // tile-local exclusive starts; s_cnt keeps the counts in a copy inside s_stage's tail
             const uint32_t n_tile = block_exclusive_scan(s_cnt, nb, s_warp);
 #pragma unroll
-            for (int j = 0; j < kScatterPer; ++j) {
+            for (int j = 0; j < kPer; ++j) {
                 if (valid[j]) {
                     const uint32_t slot = s_cnt[rec[j][half] >> shift] + rank[j];
+                    if (W == 2) {
+                        reinterpret_cast<uint2*>(s_stage)[slot] = make_uint2(rec[j][0], rec[j][1]);
+                    } else {
 #pragma unroll
-                    for (int w = 0; w < W; ++w) s_stage[slot * W + w] = rec[j][w];
+                        for (int w = 0; w < W; ++w) s_stage[slot * W + w] = rec[j][w];
+                    }
                 }
             }
             __syncthreads();
@@ -444,8 +451,12 @@ __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_
                 const uint32_t b = r[half] >> shift;
                 const uint64_t pos = base[b] + (i - s_cnt[b]);
                 uint32_t* o = reinterpret_cast<uint32_t*>(out + pos * REC);
+                if (W == 2) {  // 8-byte records: one 8-byte store
+                    *reinterpret_cast<uint2*>(o) = *reinterpret_cast<const uint2*>(r);
+                } else {
 #pragma unroll
-                for (int w = 0; w < W; ++w) o[w] = r[w];
+                    for (int w = 0; w < W; ++w) o[w] = r[w];
+                }
             }
             __syncthreads();
             // advance the block's running bases by this tile's counts (start[b+1] - start[b])
@@ -613,7 +624,7 @@ static int build_single(eg_graph* g, int want_csr, int want_csc) {
     EG_TRY(scan_exclusive_u32(g, g->bucket_cnt.as<uint32_t>(), ncnt, g->bucket_off.as<uint64_t>()));
     {
         Timed t(&g->prof, g->stream, "bucket_scatter");
-        size_t smem = sizeof(uint64_t) * 2 * pl.nb + sizeof(uint32_t) * pl.nb + (size_t)kScatterTile * rec;
+        size_t smem = align16(20ull * pl.nb) + (size_t)scatter_tile(rec) * rec;  // [2][nb] u64, [nb] u32, tile
         if (rec == 8) {
             EG_CUDA(cudaFuncSetAttribute(k_bucket_scatter<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             k_bucket_scatter<8><<<pl.nblk, kScatterThreads, smem, g->stream>>>(
@@ -783,7 +794,8 @@ int build_structures(eg_graph* g, int want_csr, int want_csc) {
 
     // the bucket tables and a staging tile must fit one CTA's shared memory
     const bool bucketed =
-        P == 1 && 20ull * plan_buckets(V, E).nb + (uint64_t)kScatterTile * g->edge_bytes <= 200ull * 1024;
+        P == 1 && align16(20ull * plan_buckets(V, E).nb) + (uint64_t)scatter_tile(g->edge_bytes) * g->edge_bytes <=
+                      200ull * 1024;
     if (bucketed) {
         // one partition: both structures (and both degree arrays) from the bucketed build
         want_csr = want_csc = 1;

@@ -26,6 +26,9 @@
 
 namespace eg {
 
+// shared-memory sub-arrays start on 16-byte boundaries (vector and 8-byte accesses)
+__host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
@@ -180,7 +183,7 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(Op op, const uint32_t* __
     extern __shared__ __align__(16) unsigned char s_raw[];
     // item boundaries relative to the chunk start, clamped to [0, chunk]: 4 bytes per item
     uint32_t* s_idx = reinterpret_cast<uint32_t*>(s_raw);
-    Acc* s_acc = reinterpret_cast<Acc*>(s_idx + cap + 1);
+    Acc* s_acc = reinterpret_cast<Acc*>(s_raw + align16(sizeof(uint32_t) * (cap + 1)));
     uint8_t* s_on = reinterpret_cast<uint8_t*>(s_acc + cap);  // per-item filter (Op::kFilter)
     for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const uint64_t e0 = c * kPullChunk;
