@@ -11,7 +11,9 @@ functionality fails loudly when the library is missing or no GPU is present.
 from __future__ import annotations
 
 import ctypes
+import functools
 import os
+import sys
 
 import numpy as np
 
@@ -172,8 +174,30 @@ def pack_edges(src, dst, w=None):
     return rec
 
 
+def _torch_ordered(fn):
+    """Order the handle's stream after torch's current stream when a CUDA tensor is passed: the
+    library runs on its own stream, and a tensor just written by torch (or still read by it) must be
+    complete before the library touches it."""
+    @functools.wraps(fn)
+    def wrapped(self, *args, **kw):
+        self._order_after_torch(list(args) + list(kw.values()))
+        return fn(self, *args, **kw)
+    return wrapped
+
+
 class Graph:
     """Graph<EdgeData> on one GPU (core/graph.hpp:100-1819)."""
+
+    def _order_after_torch(self, values):
+        torch = sys.modules.get("torch")
+        if torch is None:
+            return
+        for x in values:
+            if isinstance(x, torch.Tensor) and x.is_cuda:
+                ev = torch.cuda.Event()
+                ev.record(torch.cuda.current_stream(x.device))
+                torch.cuda.ExternalStream(self.stream, device=x.device).wait_event(ev)
+                return
 
     def __init__(self, eta=1, partitions=1, sub_partitions=1, max_iterations=20, device=0, stream=None):
         L = load_library()
@@ -212,6 +236,7 @@ class Graph:
         edges = np.ascontiguousarray(edges)
         return edges, edges.shape[0], edges.shape[1] * 4
 
+    @_torch_ordered
     def load_edges(self, edges, V, symmetric=False):
         edges, E, rec = self._records(edges)
         p, where = _buf(edges)
@@ -220,11 +245,13 @@ class Graph:
     def build(self, csr=True, csc=True):
         _check(self._L.eg_build(self.h, int(csr), int(csc)))
 
+    @_torch_ordered
     def load_directed(self, edges, V):
         edges, E, rec = self._records(edges)
         p, where = _buf(edges)
         _check(self._L.eg_load_directed(self.h, p, E, V, rec, where))
 
+    @_torch_ordered
     def load_undirected_from_directed(self, edges, V):
         edges, E, rec = self._records(edges)
         p, where = _buf(edges)
@@ -281,6 +308,7 @@ class Graph:
                     cidx=ci[:n])
 
     # ---- toolkits ------------------------------------------------------------------------------
+    @_torch_ordered
     def pagerank(self, iterations=20, damping=0.85, out=None):
         if out is None:
             out = np.empty(self.info().V, np.float32)
@@ -288,6 +316,7 @@ class Graph:
         _check(self._L.eg_pagerank(self.h, iterations, damping, p, where))
         return out
 
+    @_torch_ordered
     def bfs(self, root, level=None, parent=None, want_parent=True):
         V = self.info().V
         if level is None:
@@ -300,6 +329,7 @@ class Graph:
         _check(self._L.eg_bfs(self.h, root, pl, pp, where, ctypes.byref(reached)))
         return level, parent
 
+    @_torch_ordered
     def cc(self, label=None):
         if label is None:
             label = np.empty(self.info().V, np.uint32)
@@ -307,6 +337,7 @@ class Graph:
         _check(self._L.eg_cc(self.h, p, where))
         return label
 
+    @_torch_ordered
     def sssp(self, root, dist=None):
         if dist is None:
             dist = np.empty(self.info().V, np.float32)
@@ -314,6 +345,7 @@ class Graph:
         _check(self._L.eg_sssp(self.h, root, p, where))
         return dist
 
+    @_torch_ordered
     def load_directed_with_ids(self, edges, V):
         edges, E, rec = self._records(edges)
         if rec != 8:
@@ -321,6 +353,7 @@ class Graph:
         p, where = _buf(edges)
         _check(self._L.eg_load_directed_with_ids(self.h, p, E, V, where))
 
+    @_torch_ordered
     def msbfs(self, roots, levels=None):
         roots = np.ascontiguousarray(roots, np.uint32)
         V = self.info().V
@@ -337,6 +370,7 @@ class Graph:
         _check(self._L.eg_msbfs(self.h, rp, len(roots), p, where, ctypes.byref(e)))
         return levels, e.value
 
+    @_torch_ordered
     def sssp_batch(self, sources, dist=None):
         sources = np.ascontiguousarray(sources, np.uint32)
         V = self.info().V
@@ -351,6 +385,7 @@ class Graph:
         _check(self._L.eg_sssp_batch(self.h, sp, len(sources), p, where))
         return dist
 
+    @_torch_ordered
     def ppr(self, weights, seeds, alpha=0.15, iterations=50, out=None):
         """weights and out on the host (numpy) or all on the device (torch)."""
         seeds = np.ascontiguousarray(seeds, np.uint32)
@@ -363,6 +398,7 @@ class Graph:
         _check(self._L.eg_ppr(self.h, wp, sp, len(seeds), alpha, iterations, op, where))
         return out
 
+    @_torch_ordered
     def ppr_backward(self, weights, seeds, dl_dx, alpha=0.15, iterations=50, dl_dw=None):
         seeds = np.ascontiguousarray(seeds, np.uint32)
         if dl_dw is None:
@@ -373,6 +409,7 @@ class Graph:
                                        where))
         return dl_dw
 
+    @_torch_ordered
     def bfs_many(self, roots, levels=None):
         roots = np.ascontiguousarray(roots, np.uint32)
         p, where = _buf(levels)
@@ -387,6 +424,7 @@ class Graph:
         _check(self._L.eg_autotune(self.h, _buf(r)[0], len(r), ctypes.byref(t)))
         return t.as_dict()
 
+    @_torch_ordered
     def load_graph_batch(self, edges, graph_edges, graph_vertices):
         """edges: all graphs' records back to back; graph_edges[G+1]; graph_vertices[G]."""
         edges, E, rec = self._records(edges)
@@ -403,6 +441,7 @@ class Graph:
         _check(self._L.eg_get_graph_batch(self.h, _buf(vo)[0], _buf(eo)[0]))
         return vo, eo
 
+    @_torch_ordered
     def msbfs_graphs(self, roots, per_graph, levels=None):
         roots = np.ascontiguousarray(roots, np.uint32)
         if levels is None:
@@ -413,6 +452,7 @@ class Graph:
         _check(self._L.eg_msbfs_graphs(self.h, rp, per_graph, p, where, ctypes.byref(e)))
         return levels, e.value
 
+    @_torch_ordered
     def sssp_graphs(self, sources, per_graph, dist=None):
         sources = np.ascontiguousarray(sources, np.uint32)
         if dist is None:
@@ -474,6 +514,9 @@ def generate_rmat(out, V, E, seed, a=0.57, b=0.19, c=0.19, permute=True, weights
     L = load_library()
     rec = out.shape[1] * 4
     lo, hi = weights or (0.0, 1.0)
+    if stream is None:  # torch's stream, so that torch and the library see the records in order
+        import torch
+        stream = ctypes.c_void_p(torch.cuda.current_stream(out.device).cuda_stream)
     _check(L.eg_generate_rmat(ctypes.c_void_p(out.data_ptr()), rec, E, V, a, b, c, seed, int(permute), lo, hi,
                               stream))
     return out

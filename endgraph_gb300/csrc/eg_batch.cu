@@ -696,8 +696,8 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
                 set_error("eg_msbfs: more than 254 levels");
                 return EG_ERR_UNSUPPORTED;
             }
-            const bool dense = !g->built_csr || g->bfs_direction == 2 ||
-                               (g->bfs_direction == 0 && act >= g->E / (uint64_t)g->dense_div);
+            // the Gemini switch on the union frontier; EG_OPT_BFS_DIRECTION concerns single-root BFS
+            const bool dense = !g->built_csr || act >= g->E / (uint64_t)g->dense_div;
             uint32_t nout = 0;
             // a bitmap test before each gather pays only while the frontier is a small part of V
             EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act));

@@ -1,16 +1,8 @@
-// eg_pull.cuh — the traversal machinery shared by the toolkits (eg_engine.cu) and the batched
-// operators (eg_batch.cu): the chunked pull sweep over the compressed CSC, the rank-balanced push
-// expansion over a frontier queue, and their host-side launchers.
-//
-// Push (sparse, core/graph.hpp:1505-1655): the frontier is a queue of vertices; a look-back scan
-// over the frontier's list lengths gives every frontier edge a global rank, and the expansion
-// kernel hands each CTA a fixed run of 2048 ranks (8 contiguous edges per thread), so hubs and
-// leaves cost the same per edge.  Activations are de-duplicated in a bitmap and appended with
-// warp-aggregated atomics.
-// Pull (dense, :1656-1802): the CSC is swept in fixed 4096-edge chunks (16 contiguous ids per
-// thread, 128-bit loads); a chunk's compressed entries are staged in shared memory and each thread
-// reduces its edges per destination into shared accumulators.  Destinations wholly inside a chunk
-// are finalised in place; the few whose list crosses a chunk boundary are combined afterwards.
+// eg_pull.cuh — host-side launchers of the traversal kernels (include/endgraph_gb300_kernels.cuh)
+// on a graph handle: pull setup (first compressed entry per 4096-edge chunk, entries crossing
+// chunks), the chunked pull sweeps, engine scratch, and one push level over a frontier queue
+// (look-back rank of the frontier's edges, then the rank-balanced expansion).  Shared by the
+// toolkits (eg_engine.cu) and the batched operators (eg_batch.cu).
 #pragma once
 
 #include <algorithm>

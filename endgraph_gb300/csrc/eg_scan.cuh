@@ -1,11 +1,5 @@
-// eg_scan.cuh — single-pass prefix scan (decoupled look-back) over u32 items with u64 sums.
-//
-// Each 256-thread CTA takes the next 4096-item tile from a ticket counter (so every tile it waits
-// on belongs to a CTA that is already running), loads the tile striped (coalesced) into shared
-// memory, scans it, publishes its aggregate, looks back over predecessor descriptors with warp 0,
-// publishes its inclusive prefix and hands (index, exclusive prefix, value) of every item to an
-// epilogue functor.  Descriptor: status in bits 63..62 (1 aggregate, 2 inclusive), value in 61..0.
-// The look-back spin is bounded: on exhaustion the CTA raises err[0] and publishes anyway.
+// eg_scan.cuh — host launcher of the decoupled look-back scan (k_scan, in
+// include/endgraph_gb300_kernels.cuh) on a graph handle's scratch and stream.
 #pragma once
 
 #include "eg_common.cuh"

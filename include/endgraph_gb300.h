@@ -165,9 +165,10 @@ int eg_sssp(eg_graph* g, uint32_t root, float* dist, int where);
 
 /* Engine options.  EG_OPT_DENSE_DIVISOR: process_edges runs sparse (push) iff the active
  * vertices' out-edges < E / divisor (core/graph.hpp:1484-1491; the reference uses 20).
- * EG_OPT_BFS_DIRECTION: 0 applies that switch to BFS with the toolkit's dense callbacks
- * (toolkits/bfs.cpp:60-76), 1 forces push every level as the reference's use_root flag does
- * (core/graph.hpp:1496-1498), 2 forces pull.  Results are identical in every mode.
+ * EG_OPT_BFS_DIRECTION: 0 applies that switch to single-root BFS with the toolkit's dense
+ * callbacks (toolkits/bfs.cpp:60-76), 1 forces push every level as the reference's use_root flag
+ * does (core/graph.hpp:1496-1498), 2 forces pull.  Results are identical in every mode.  The
+ * bit-parallel BFS always switches on its union frontier with the same divisor.
  * EG_OPT_CUDA_GRAPH: 1 replays the batched-BFS level loop (eg_msbfs, eg_msbfs_graphs) as one
  * captured CUDA graph of 32 levels instead of one host round trip per level. */
 enum {
