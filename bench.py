@@ -199,7 +199,28 @@ ALG_BYTES = {  # algorithmic bytes per launch (E edges, V vertices, nc compresse
     "bitmap": lambda E, V, nc: 4 * V + V // 8,
     "cpbt_page_weights": lambda E, V, nc: 4 * V,
     "pr_pull": lambda E, V, nc: 8 * E + 16 * nc,
+    "bucket_hist": lambda E, V, nc: 8 * E,
+    "bucket_scatter": lambda E, V, nc: 24 * E,
+    "bucket_build": lambda E, V, nc: 12 * E + 12 * V,
 }
+
+
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "dram_traffic_rmat-s25-ef16.md")
+
+
+def profiled_traffic(args):
+    """DRAM bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum) of the bench's
+    kernels, from the committed summary of a capture of this workload: rows
+    `| `bench name` | kernel | launches | read GB | write GB | bytes per launch |`."""
+    if args.scale != 25 or args.edge_factor != 16 or not os.path.exists(TRAFFIC_PROFILE):
+        return {}
+    out = {}
+    with open(TRAFFIC_PROFILE) as f:
+        for line in f:
+            cols = [c.strip() for c in line.strip().strip("|").split("|")]
+            if len(cols) == 6 and cols[0].startswith("`") and cols[5].isdigit():
+                out[cols[0].strip("`")] = int(cols[5])
+    return out
 
 
 def _timed(stream, fn):
@@ -490,13 +511,7 @@ def run_ours(args, world, rank, local):
     achieved = None
     if alg:
         achieved = alg(E, V, nc) / (ms_dom / n_dom / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            tr = json.load(f)
-        if dom in tr:
-            traffic = tr[dom].get("bytes_per_launch_at_bench")
+    traffic = profiled_traffic(args).get(dom)
     prep_bytes = 24 * E + 32 * V
     pr_bytes = args.pr_iters * (8 * E + 20 * V)
     kernels = {k: {"launches": n, "ms_total": round(ms, 3), "ms_per_launch": round(ms / n, 4),
