@@ -2,7 +2,7 @@
 // operator API of endgraph_gb300_engine.cuh, in the reference's own shape: signal/slot pairs passed
 // to process_edges, vertex updates through process_vertices, the same iteration structure.
 //
-//   engine_toolkits pagerank|bfs|cc|sssp <edge file> <V> <iterations|root> <out file>
+//   engine_toolkits pagerank|bfs|cc|sssp <edge file> <V> <iterations|root> <out file> [partitions]
 //
 // Writes the result array (double ranks, u32 levels + u32 parents, u32 labels, f32 distances)
 // to <out file> for the test to compare with the oracle.
@@ -199,7 +199,8 @@ int main(int argc, char** argv) {
     const int rec = algo == "sssp" ? 12 : 8;
     std::vector<char> buf = read_file(argv[2]);
     const uint64_t E = buf.size() / rec;
-    eg_config cfg = {1, 1, 1, 20, 0, nullptr};
+    const int parts = argc > 6 ? atoi(argv[6]) : 1;  // CPBT partitions (virtual, on this GPU)
+    eg_config cfg = {1, parts, 1, 20, 0, nullptr};
     eg_graph* h = nullptr;
     eg::engine::check_eg(eg_create(&h, &cfg), "eg_create");
     eg::engine::check_eg(eg_load_edges(h, buf.data(), E, V, rec, algo == "cc" ? 1 : 0, EG_HOST), "eg_load_edges");

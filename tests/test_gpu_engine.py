@@ -36,21 +36,22 @@ def engine_exe(tmp_path_factory):
     return _compile(str(tmp_path_factory.mktemp("engine") / "engine_toolkits"))
 
 
-def _run(exe, tmp_path, algo, rec, V, arg):
+def _run(exe, tmp_path, algo, rec, V, arg, partitions=1):
     f = tmp_path / f"{algo}.bin"
     rec.tofile(f)
     out = tmp_path / f"{algo}.out"
-    r = subprocess.run([exe, algo, str(f), str(V), str(arg), str(out)], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([exe, algo, str(f), str(V), str(arg), str(out), str(partitions)], capture_output=True,
+                       text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     return out, r.stdout
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("V,E,seed", [(1 << 14, 1 << 18, 5), (100_000, 600_000, 6)])
-def test_engine_pagerank_fp64(engine_exe, tmp_path, V, E, seed):
+@pytest.mark.parametrize("V,E,seed,P", [(1 << 14, 1 << 18, 5, 1), (100_000, 600_000, 6, 1), (100_000, 600_000, 6, 3)])
+def test_engine_pagerank_fp64(engine_exe, tmp_path, V, E, seed, P):
     import endgraph_gb300 as eg
     src, dst, _ = rmat_graph(V, E, seed)
-    out, _ = _run(engine_exe, tmp_path, "pagerank", eg.pack_edges(src, dst), V, 20)
+    out, _ = _run(engine_exe, tmp_path, "pagerank", eg.pack_edges(src, dst), V, 20, P)
     pr = np.fromfile(out, np.float64)
     o_out, _ = oracle.degrees(src, dst, V)
     csc = oracle.build_csc(src, dst, None, V, np.array([0, V], np.uint32))
@@ -59,12 +60,12 @@ def test_engine_pagerank_fp64(engine_exe, tmp_path, V, E, seed):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("V,E,seed", [(1 << 14, 1 << 18, 7), (1 << 16, 1 << 20, 8)])
-def test_engine_bfs(engine_exe, tmp_path, V, E, seed):
+@pytest.mark.parametrize("V,E,seed,P", [(1 << 14, 1 << 18, 7, 1), (1 << 16, 1 << 20, 8, 1), (1 << 16, 1 << 20, 8, 2)])
+def test_engine_bfs(engine_exe, tmp_path, V, E, seed, P):
     import endgraph_gb300 as eg
     src, dst, _ = rmat_graph(V, E, seed)
     root = int(src[0])
-    out, log = _run(engine_exe, tmp_path, "bfs", eg.pack_edges(src, dst), V, root)
+    out, log = _run(engine_exe, tmp_path, "bfs", eg.pack_edges(src, dst), V, root, P)
     a = np.fromfile(out, np.uint32)
     lv, par = a[:V], a[V:]
     csr = oracle.build_csr(src, dst, None, V, np.array([0, V], np.uint32))
@@ -74,11 +75,11 @@ def test_engine_bfs(engine_exe, tmp_path, V, E, seed):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("V,E,seed", [(1 << 14, 1 << 17, 9), (100_000, 300_000, 10)])
-def test_engine_cc(engine_exe, tmp_path, V, E, seed):
+@pytest.mark.parametrize("V,E,seed,P", [(1 << 14, 1 << 17, 9, 1), (100_000, 300_000, 10, 1), (100_000, 300_000, 10, 4)])
+def test_engine_cc(engine_exe, tmp_path, V, E, seed, P):
     import endgraph_gb300 as eg
     src, dst, _ = rmat_graph(V, E, seed)
-    out, _ = _run(engine_exe, tmp_path, "cc", eg.pack_edges(src, dst), V, 0)
+    out, _ = _run(engine_exe, tmp_path, "cc", eg.pack_edges(src, dst), V, 0, P)
     assert np.array_equal(np.fromfile(out, np.uint32), oracle.cc_labels(src, dst, V))
 
 
