@@ -450,6 +450,10 @@ int eg_set_option(eg_graph* g, int option, int64_t value) {
             if (value < 1 || value > 64) break;
             g->batch_width = (int)value;
             return EG_OK;
+        case EG_OPT_SSSP_DELTA:
+            if (value < -1 || value > (1ll << 40)) break;
+            g->sssp_delta = value;
+            return EG_OK;
         default:
             set_error("eg_set_option: unknown option %d", option);
             return EG_ERR_INVALID;

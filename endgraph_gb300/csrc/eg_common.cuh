@@ -177,6 +177,7 @@ struct eg_graph {
     int use_cuda_graph = 0; // batched BFS: replay the level loop as one captured CUDA graph
     int pull_blocks_per_sm = 0;  // pull-sweep grid; 0 = occupancy limit
     int batch_width = 64;        // roots per bit-parallel pass (eg_bfs_many)
+    int64_t sssp_delta = -1;     // SSSP near/far step in millionths; 0 = Bellman-Ford, -1 = automatic
     // many small graphs in one handle (eg_load_graph_batch): per-graph vertex / edge offsets
     std::vector<uint64_t> batch_voff, batch_eoff;
     eg::DevBuf d_batch_voff;

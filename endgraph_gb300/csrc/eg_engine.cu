@@ -9,6 +9,7 @@
 // thread, 128-bit loads); a chunk's compressed entries are staged in shared memory and each thread
 // reduces its edges per destination into shared accumulators.  Destinations wholly inside a chunk
 // are finalised in place; the few whose list crosses a chunk boundary are combined afterwards.
+#include <math.h>
 #include <string.h>
 
 #include <algorithm>
@@ -160,10 +161,17 @@ __global__ void __launch_bounds__(256) k_bu_tail(BuArgs a) {
     }
 }
 
-struct SsspOp {  // toolkits/sssp.cpp:52-64: relax_dist = dist[src] + w; write_min
+// toolkits/sssp.cpp:52-64: relax_dist = dist[src] + w; write_min.  With a near/far split a
+// lowered vertex joins the next frontier only if its distance is below the current threshold;
+// otherwise it is parked in the far bitmap until the threshold passes it.  Every relaxation is
+// the reference's, only their order changes, and the least fixpoint of the float relaxations is
+// unique, so distances are the same bit for bit.
+struct SsspOp {
     float* dist;
     const float* wts;
     unsigned long long* next_bm;
+    unsigned long long* far_bm;  // nullptr: plain Bellman-Ford sweeps
+    float thr;
     __device__ uint32_t payload(uint32_t u) const { return __float_as_uint(__ldcg(dist + u)); }
     __device__ bool relax(uint32_t, uint32_t pay, uint32_t w, uint64_t pos) const {
         const float nd = __uint_as_float(pay) + wts[pos];
@@ -171,9 +179,62 @@ struct SsspOp {  // toolkits/sssp.cpp:52-64: relax_dist = dist[src] + w; write_m
         const int old = atomicMin(reinterpret_cast<int*>(dist + w), __float_as_int(nd));
         if (!(nd < __int_as_float(old))) return false;
         const unsigned long long bit = 1ull << (w & 63);
+        if (far_bm && !(nd < thr)) {
+            if (!(__ldcg(far_bm + (w >> 6)) & bit)) atomicOr(far_bm + (w >> 6), bit);
+            return false;
+        }
         return !(atomicOr(next_bm + (w >> 6), bit) & bit);
     }
 };
+
+// far vertices whose distance is now below thr move to the near queue; the others stay, and
+// their smallest distance (non-negative floats order like their bit patterns) and count are
+// reported so that an empty phase can jump straight to the next occupied one
+__global__ void k_far_split(unsigned long long* far_bm, uint64_t nwords, const float* __restrict__ dist, float thr,
+                            uint32_t* q, uint32_t* nq, unsigned int* min_far_bits, unsigned int* n_far) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < nwords; base += stride) {
+        const uint64_t w = base + lane;
+        const unsigned long long word = w < nwords ? far_bm[w] : 0ull;
+        unsigned long long move = 0;
+        unsigned int mn = 0x7F800000u, left = 0;  // +inf
+        for (unsigned long long x = word; x;) {
+            const int b = __ffsll((long long)x) - 1;
+            x &= x - 1;
+            const float d = __ldcg(dist + w * 64 + b);
+            if (d < thr) {
+                move |= 1ull << b;
+            } else {
+                ++left;
+                mn = min(mn, __float_as_uint(d));
+            }
+        }
+        if (move) far_bm[w] = word & ~move;
+        const uint32_t cnt = (uint32_t)__popcll(move);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            left += __shfl_xor_sync(0xffffffffu, left, o);
+        }
+        if (lane == 0 && left) {
+            atomicMin(min_far_bits, mn);
+            atomicAdd(n_far, left);
+        }
+        if (!tot) continue;
+        uint32_t at = 0;
+        if (lane == 31) at = atomicAdd(nq, tot);
+        at = __shfl_sync(0xffffffffu, at, 31) + incl - cnt;
+        for (unsigned long long x = move; x; x &= x - 1) q[at++] = (uint32_t)(w * 64 + (uint64_t)(__ffsll((long long)x) - 1));
+    }
+}
 
 struct CcPushOp {  // toolkits/cc.cpp:50-60: msg = label[src]; write_min(label[dst], msg)
     uint32_t* label;
@@ -470,6 +531,18 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
     return EG_OK;
 }
 
+// mean of a strided sample of the weights, for the automatic near/far threshold step
+__global__ void k_weight_sample(const float* __restrict__ w, uint64_t E, uint64_t step, uint32_t n, float* out) {
+    float acc = 0.f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t e = (uint64_t)i * step;
+        if (e < E) acc += w[e];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
 int run_sssp(eg_graph* g, uint32_t root, float* dist, int where) {
     if (!g->built_csr) { set_error("eg_sssp: CSR not built"); return EG_ERR_STATE; }
     if (!g->weighted) { set_error("eg_sssp: graph has no edge weights (load 12-byte records)"); return EG_ERR_STATE; }
@@ -478,29 +551,84 @@ int run_sssp(eg_graph* g, uint32_t root, float* dist, int where) {
     const uint32_t V = g->V;
     EngineState& s = g->eng;
     float* d_dist = s.vals0.as<float>();
-    const size_t bm_bytes = sizeof(uint64_t) * (V / 64 + 1);
+    const uint64_t nwords = (uint64_t)V / 64 + 1;
+    const size_t bm_bytes = sizeof(uint64_t) * nwords;
+    unsigned long long* far_bm = s.bm_visit.as<unsigned long long>();
+    unsigned int* d_small = reinterpret_cast<unsigned int*>(s.counters.as<unsigned long long>() + 6);
     {
         Timed t(&g->prof, g->stream, "sssp_init");
         k_fill_f32<<<grid_for(V, 256, 152u * 16u), 256, 0, g->stream>>>(d_dist, V, 1e9f);
         EG_CHECK_LAUNCH("k_fill_f32");
         EG_CUDA(cudaMemsetAsync(s.bm_next.ptr, 0, bm_bytes, g->stream));
+        EG_CUDA(cudaMemsetAsync(far_bm, 0, bm_bytes, g->stream));
         k_sssp_root<<<1, 1, 0, g->stream>>>(d_dist, root, s.q0.as<uint32_t>());
         EG_CHECK_LAUNCH("k_sssp_root");
     }
+    // threshold step: the option (millionths), or 0.7 x mean weight / mean out-degree (the best
+    // of a sweep on the 41.6 M-vertex, 1.47 B-edge R-MAT: 0.01 there, 2.3x faster than plain
+    // sweeps), or none
+    float delta = 0.f;
+    if (g->sssp_delta > 0) {
+        delta = (float)((double)g->sssp_delta * 1e-6);
+    } else if (g->sssp_delta < 0 && g->E > 0) {
+        const uint32_t ns = 65536;
+        const uint64_t step = std::max<uint64_t>(g->E / ns, 1);
+        float* d_sum = reinterpret_cast<float*>(d_small);
+        EG_CUDA(cudaMemsetAsync(d_sum, 0, 4, g->stream));
+        k_weight_sample<<<64, 256, 0, g->stream>>>(g->csr_w.as<float>(), g->E, step, ns, d_sum);
+        EG_CHECK_LAUNCH("k_weight_sample");
+        float sum = 0.f;
+        EG_CUDA(cudaMemcpyAsync(&sum, d_sum, 4, cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaStreamSynchronize(g->stream));
+        const uint64_t taken = std::min<uint64_t>(ns, (g->E + step - 1) / step);
+        const double mean_w = taken ? sum / (double)taken : 0.0;
+        const double mean_deg = (double)g->E / (double)V;
+        delta = (float)(mean_w * 0.7 / std::max(mean_deg, 1.0));
+    }
+    const bool split = delta > 0.f;
+    float thr = split ? delta : INFINITY;
     uint32_t* qa = s.q0.as<uint32_t>();
     uint32_t* qb = s.q1.as<uint32_t>();
     uint64_t n = 1, total_edges = 0;
-    int iters = 0;
-    while (n > 0) {
-        SsspOp op{d_dist, g->csr_w.as<float>(), s.bm_next.as<unsigned long long>()};
-        uint32_t nout = 0;
-        uint64_t T = 0;
-        EG_TRY(push_level(g, op, qa, n, qb, &nout, &T, nullptr, nullptr, "sssp_push"));
-        EG_CUDA(cudaMemsetAsync(s.bm_next.ptr, 0, bm_bytes, g->stream));
-        total_edges += T;
-        std::swap(qa, qb);
-        n = nout;
-        ++iters;
+    int iters = 0, phases = 1;
+    while (true) {
+        while (n > 0) {
+            SsspOp op{d_dist, g->csr_w.as<float>(), s.bm_next.as<unsigned long long>(), split ? far_bm : nullptr, thr};
+            uint32_t nout = 0;
+            uint64_t T = 0;
+            EG_TRY(push_level(g, op, qa, n, qb, &nout, &T, nullptr, nullptr, "sssp_push"));
+            EG_CUDA(cudaMemsetAsync(s.bm_next.ptr, 0, bm_bytes, g->stream));
+            total_edges += T;
+            std::swap(qa, qb);
+            n = nout;
+            ++iters;
+        }
+        if (!split) break;
+        // next phase: raise the threshold by delta, or to the nearest parked distance + delta
+        struct {
+            unsigned int nq, min_bits, n_far, pad;
+        } h = {0, 0, 0, 0};
+        float next = thr + delta;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            const unsigned int init[4] = {0u, 0x7F800000u, 0u, 0u};
+            EG_CUDA(cudaMemcpyAsync(d_small, init, 16, cudaMemcpyHostToDevice, g->stream));
+            {
+                Timed t(&g->prof, g->stream, "sssp_far_split");
+                k_far_split<<<grid_for(nwords, 256, (unsigned)g->num_sms * 8u), 256, 0, g->stream>>>(
+                    far_bm, nwords, d_dist, next, qa, d_small, d_small + 1, d_small + 2);
+                EG_CHECK_LAUNCH("k_far_split");
+            }
+            EG_CUDA(cudaMemcpyAsync(&h, d_small, 16, cudaMemcpyDeviceToHost, g->stream));
+            EG_CUDA(cudaStreamSynchronize(g->stream));
+            if (h.nq > 0 || h.n_far == 0) break;
+            float mn;
+            memcpy(&mn, &h.min_bits, 4);
+            next = std::max(next, mn) + delta;  // skip the empty phases
+        }
+        thr = next;
+        n = h.nq;
+        ++phases;
+        if (n == 0) break;  // nothing parked: done
     }
     EG_TRY(copy_out(g, dist, d_dist, sizeof(float) * (size_t)V, where));
     EG_CUDA(cudaStreamSynchronize(g->stream));

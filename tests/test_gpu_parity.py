@@ -132,11 +132,13 @@ def test_cc(eg_lib, V, E, seed):
 
 
 @pytest.mark.parametrize("V,E,seed", CASES)
-def test_sssp(eg_lib, V, E, seed):
+@pytest.mark.parametrize("delta", [-1, 0, 50_000])  # automatic near/far step, plain sweeps, 0.05
+def test_sssp(eg_lib, V, E, seed, delta):
     import endgraph_gb300 as eg
     src, dst, w = rmat_graph(V, E, seed, weights=(0.0, 1.0))
     csr = oracle.build_csr(src, dst, w, V, np.array([0, V], np.uint32))
     with _graph(eg_lib) as g:
+        g.set_option(eg.EG_OPT_SSSP_DELTA, delta)
         g.load_directed(eg.pack_edges(src, dst, w), V)
         for root in [int(src[0]), int(src[7])]:
             ref = oracle.sssp(csr["off"][0], csr["adj"], csr["w"], V, root)
