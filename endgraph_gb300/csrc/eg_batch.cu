@@ -407,13 +407,45 @@ __global__ void __launch_bounds__(256) k_row_sssp(RowArgs a, float2* __restrict_
         const uint64_t e0 = lb + (uint64_t)a.t_part[t] * kTaskEdges;
         const uint64_t e1 = e0 + kTaskEdges < le ? e0 + kTaskEdges : le;
         float2 best = make_float2(1e9f, 1e9f);
-        for (uint64_t e = e0; e < e1; ++e) {
-            const uint32_t u = __ldg(a.adj + e);
-            if (!__ldcg(changed_prev + u)) continue;  // uniform across the warp
-            const float wv = __ldg(a.w + e);
-            const float2 du = __ldcg(dist + (uint64_t)u * 32 + lane);
-            best.x = fminf(best.x, du.x + wv);  // toolkits/sssp.cpp:55: relax_dist = msg + w
-            best.y = fminf(best.y, du.y + wv);
+        // 32 in-edges per step: ids, weights and "source changed" flags are loaded one per lane,
+        // then the rows of the changed sources are gathered four at a time (min is exact, so the
+        // order does not matter)
+        for (uint64_t eb = e0; eb < e1; eb += 32) {
+            const uint64_t e = eb + lane;
+            uint32_t u = 0;
+            float wv = 0.f;
+            bool ch = false;
+            if (e < e1) {
+                u = __ldg(a.adj + e);
+                wv = __ldg(a.w + e);
+                ch = __ldcg(changed_prev + u) != 0;
+            }
+            unsigned m = __ballot_sync(0xffffffffu, ch);
+            while (m) {  // m is the same in every lane
+                int sl[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    sl[j] = m ? __ffs(m) - 1 : -1;
+                    if (m) m &= m - 1;
+                }
+                float2 r[4];
+                float wj[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (sl[j] >= 0) {
+                        const uint32_t uj = __shfl_sync(0xffffffffu, u, sl[j]);
+                        wj[j] = __shfl_sync(0xffffffffu, wv, sl[j]);
+                        r[j] = __ldcg(dist + (uint64_t)uj * 32 + lane);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (sl[j] >= 0) {
+                        best.x = fminf(best.x, r[j].x + wj[j]);  // toolkits/sssp.cpp:55: relax_dist = msg + w
+                        best.y = fminf(best.y, r[j].y + wj[j]);
+                    }
+                }
+            }
         }
         const uint32_t v = a.item_vertex[it];
         float2* dv = dist + (uint64_t)v * 32 + lane;
