@@ -1,8 +1,14 @@
 // eg_api.cu — the extern "C" boundary of libendgraph_gb300.so (include/endgraph_gb300.h).
+#include <errno.h>
+#include <fcntl.h>
 #include <string.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <memory>
+#include <thread>
+#include <vector>
 
 #include "eg_common.cuh"
 
@@ -118,6 +124,11 @@ int eg_load_edges(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int ed
     return load_edges_impl(g, edges, E, V, edge_bytes, symmetric, where, true);
 }
 
+int eg_load_file(eg_graph* g, const char* path, uint32_t V, int edge_bytes, int symmetric) {
+    EG_TRY(check_graph(g, "eg_load_file"));
+    return load_file_impl(g, path, V, edge_bytes, symmetric);
+}
+
 int eg_load_graph_batch(eg_graph* g, const void* edges, int edge_bytes, const uint64_t* graph_edges,
                         const uint32_t* graph_vertices, int ngraphs, int where) {
     EG_TRY(check_graph(g, "eg_load_graph_batch"));
@@ -149,22 +160,36 @@ int eg_sssp_graphs(eg_graph* g, const uint32_t* sources, int sources_per_graph, 
 }  // extern "C"
 
 namespace eg {
+static int prepare_load(eg_graph* g, uint64_t E, uint32_t V, int edge_bytes, int symmetric);
+
 int load_edges_impl(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int symmetric, int where,
                     bool validate) {
-    if (edge_bytes != 8 && edge_bytes != 12) {
-        set_error("eg_load_edges: edge_bytes must be 8 ({src,dst}) or 12 ({src,dst,float})");
-        return EG_ERR_INVALID;
-    }
-    if (V == 0) {
-        set_error("eg_load_edges: V must be positive");
-        return EG_ERR_INVALID;
-    }
     if (E > 0 && !edges) {
         set_error("eg_load_edges: null edge pointer");
         return EG_ERR_INVALID;
     }
     if (where != EG_HOST && where != EG_DEVICE) {
         set_error("eg_load_edges: where must be EG_HOST or EG_DEVICE");
+        return EG_ERR_INVALID;
+    }
+    EG_TRY(prepare_load(g, E, V, edge_bytes, symmetric));
+    if (E) {
+        EG_CUDA(cudaMemcpyAsync(g->edges.ptr, edges, (size_t)E * edge_bytes,
+                                where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, g->stream));
+    }
+    if (validate) EG_TRY(validate_edges(g, E));
+    if (symmetric) EG_TRY(symmetrize_edges(g, E));
+    return EG_OK;
+}
+
+// argument checks, state reset and the record buffer of a new edge list
+static int prepare_load(eg_graph* g, uint64_t E, uint32_t V, int edge_bytes, int symmetric) {
+    if (edge_bytes != 8 && edge_bytes != 12) {
+        set_error("eg_load_edges: edge_bytes must be 8 ({src,dst}) or 12 ({src,dst,float})");
+        return EG_ERR_INVALID;
+    }
+    if (V == 0) {
+        set_error("eg_load_edges: V must be positive");
         return EG_ERR_INVALID;
     }
     const uint64_t total = symmetric ? 2 * E : E;
@@ -185,11 +210,112 @@ int load_edges_impl(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int 
     g->weighted = edge_bytes == 12;
     g->symmetric = symmetric != 0;
     EG_TRY(g->edges.reserve((size_t)total * edge_bytes + 64));
-    if (E) {
-        EG_CUDA(cudaMemcpyAsync(g->edges.ptr, edges, (size_t)E * edge_bytes,
-                                where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, g->stream));
+    return EG_OK;
+}
+
+// preload_graph_file (core/graph.hpp:1011-1084) for one rank: the whole file, read in 64 MiB
+// pieces into two pinned staging buffers, so that reading piece i+1 overlaps the host-to-device
+// copy of piece i; then the same validation and symmetrisation as eg_load_edges.
+constexpr size_t kIngestPiece = 64ull << 20;
+
+int load_file_impl(eg_graph* g, const char* path, uint32_t V, int edge_bytes, int symmetric) {
+    if (!path) {
+        set_error("eg_load_file: null path");
+        return EG_ERR_INVALID;
     }
-    if (validate) EG_TRY(validate_edges(g, E));
+    const int fd = open(path, O_RDONLY);
+    if (fd < 0) {
+        set_error("eg_load_file: cannot open %s", path);
+        return EG_ERR_INVALID;
+    }
+    struct stat st;
+    if (fstat(fd, &st) != 0 || st.st_size < 0) {
+        close(fd);
+        set_error("eg_load_file: cannot stat %s", path);
+        return EG_ERR_INVALID;
+    }
+    const uint64_t bytes = (uint64_t)st.st_size;
+    if (edge_bytes > 0 && bytes % (uint64_t)edge_bytes) {
+        close(fd);
+        set_error("eg_load_file: %s holds %llu bytes, not a whole number of %d-byte records", path,
+                  (unsigned long long)bytes, edge_bytes);
+        return EG_ERR_INVALID;
+    }
+    const uint64_t E = edge_bytes > 0 ? bytes / (uint64_t)edge_bytes : 0;
+    int st_load = prepare_load(g, E, V, edge_bytes, symmetric);
+    if (st_load != EG_OK) {
+        close(fd);
+        return st_load;
+    }
+    if (g->pinned_bytes < 2 * kIngestPiece) {
+        if (g->pinned) cudaFreeHost(g->pinned);
+        g->pinned = nullptr;
+        g->pinned_bytes = 0;
+        cudaError_t e = cudaHostAlloc(&g->pinned, 2 * kIngestPiece, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            close(fd);
+            g->pinned = nullptr;
+            return cuda_fail(e, "cudaHostAlloc", __FILE__, __LINE__);
+        }
+        g->pinned_bytes = 2 * kIngestPiece;
+    }
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    int status = EG_OK;
+    for (int i = 0; i < 2 && status == EG_OK; ++i) {
+        cudaError_t e = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
+        if (e != cudaSuccess) status = cuda_fail(e, "cudaEventCreate", __FILE__, __LINE__);
+    }
+    uint8_t* dst = g->edges.as<uint8_t>();
+    for (uint64_t off = 0, piece = 0; status == EG_OK && off < bytes; off += kIngestPiece, ++piece) {
+        const int slot = (int)(piece & 1);
+        uint8_t* buf = static_cast<uint8_t*>(g->pinned) + slot * kIngestPiece;
+        if (piece >= 2) {  // the copy that last used this buffer must have finished
+            cudaError_t e = cudaEventSynchronize(done[slot]);
+            if (e != cudaSuccess) {
+                status = cuda_fail(e, "cudaEventSynchronize", __FILE__, __LINE__);
+                break;
+            }
+        }
+        const size_t n = (size_t)std::min<uint64_t>(kIngestPiece, bytes - off);
+        // the piece is read by several threads at once (page-cache copies are per-thread bound)
+        const unsigned nt = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+        const size_t part = (n + nt - 1) / nt;
+        std::vector<size_t> got(nt, 0);
+        std::vector<std::thread> readers;
+        for (unsigned t = 0; t < nt; ++t) {
+            const size_t a = std::min(n, t * part), z = std::min(n, a + part);
+            readers.emplace_back([&, t, a, z]() {
+                size_t done_t = 0;
+                while (a + done_t < z) {
+                    const ssize_t r = pread(fd, buf + a + done_t, z - a - done_t, (off_t)(off + a + done_t));
+                    if (r < 0 && errno == EINTR) continue;
+                    if (r <= 0) break;
+                    done_t += (size_t)r;
+                }
+                got[t] = (a + done_t == z) ? 1 : 0;
+            });
+        }
+        for (auto& th : readers) th.join();
+        bool whole = true;
+        for (unsigned t = 0; t < nt; ++t) whole = whole && got[t];
+        if (!whole) {
+            set_error("eg_load_file: short read of %s in the piece at byte %llu", path, (unsigned long long)off);
+            status = EG_ERR_INVALID;
+            break;
+        }
+        cudaError_t e = cudaMemcpyAsync(dst + off, buf, n, cudaMemcpyHostToDevice, g->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(done[slot], g->stream);
+        if (e != cudaSuccess) status = cuda_fail(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+    }
+    close(fd);
+    cudaStreamSynchronize(g->stream);  // the staging buffers may be reused by the next call
+    for (int i = 0; i < 2; ++i)
+        if (done[i]) cudaEventDestroy(done[i]);
+    if (status != EG_OK) {
+        g->V = 0;  // no usable edge list
+        return status;
+    }
+    EG_TRY(validate_edges(g, E));
     if (symmetric) EG_TRY(symmetrize_edges(g, E));
     return EG_OK;
 }

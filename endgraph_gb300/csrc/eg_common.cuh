@@ -214,6 +214,7 @@ int run_sssp_batch(eg_graph* g, const uint32_t* srcs, int n, float* out, int whe
 void free_batch_state(eg_graph* g);
 int load_edges_impl(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int symmetric, int where,
                     bool validate);
+int load_file_impl(eg_graph* g, const char* path, uint32_t V, int edge_bytes, int symmetric);
 int load_graph_batch(eg_graph* g, const void* edges, int rec, const uint64_t* eoff, const uint32_t* nverts, int G,
                      int where);
 int run_msbfs_graphs(eg_graph* g, const uint32_t* roots, int nper, uint8_t* levels, int where, uint64_t* edges);

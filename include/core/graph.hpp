@@ -3,8 +3,9 @@
 //
 // The reference's toolkits (toolkits/{pagerank,bfs,cc,sssp}.cpp) compile unchanged against this
 // header: it keeps the names, signatures, public fields and types they use.  What runs:
-//   - load_directed / load_undirected_from_directed read the binary edge file and build CPBT
-//     partition + CSR + CSC on the GPU; prep_time times the build only (like :1367-1371);
+//   - load_directed / load_undirected_from_directed stream the binary edge file to the GPU
+//     (eg_load_file) and build CPBT partition + CSR + CSC there; prep_time times the build only
+//     (like :1367-1371);
 //   - vertex arrays, subsets, gather/dump/restore are host-side helpers as in the reference;
 //   - the toolkits themselves run on the GPU through pagerank() / bfs() / cc() / sssp();
 //   - process_vertices / process_edges / emit with host std::function callbacks are accepted by the
@@ -179,29 +180,14 @@ class Graph {
     }
 
     void load(const std::string& path, UINT vertices, bool symmetric) {
-        long bytes = file_size(path);
-        if (bytes < 0) throw EndGraphError(EG_ERR_INVALID, "cannot stat " + path);
         const size_t rec = sizeof(EdgeType<EdgeData>);
-        const ULLONG n = (ULLONG)bytes / rec;
-        std::vector<char> buf(n * rec + 1);
-        int fd = open(path.c_str(), O_RDONLY);
-        if (fd < 0) throw EndGraphError(EG_ERR_INVALID, "cannot open " + path);
-        size_t done = 0;
-        while (done < n * rec) {  // CHUNKSIZE records per read, like preload_graph_file
-            size_t want = n * rec - done;
-            if (want > (size_t)CHUNKSIZE * rec) want = (size_t)CHUNKSIZE * rec;
-            ssize_t got = read(fd, buf.data() + done, want);
-            if (got <= 0) break;
-            done += (size_t)got;
-        }
-        close(fd);
-        if (done != n * rec) throw EndGraphError(EG_ERR_INVALID, "short read " + path);
+        eg_throw_if(eg_load_file(handle_, path.c_str(), vertices, (int)rec, symmetric ? 1 : 0), "eg_load_file");
+        eg_info info;
+        eg_throw_if(eg_get_info(handle_, &info), "eg_get_info");
         vertices_num = vertices;
-        edges_num = symmetric ? 2 * n : n;
+        edges_num = info.E;
         read_edges_num = edges_num;
         owned_vertices = vertices;
-        eg_throw_if(eg_load_edges(handle_, buf.data(), n, vertices, (int)rec, symmetric ? 1 : 0, EG_HOST),
-                    "eg_load_edges");
         double t = -MPI_Wtime();
         eg_throw_if(eg_build(handle_, 1, 1), "eg_build");
         t += MPI_Wtime();

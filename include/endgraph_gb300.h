@@ -104,6 +104,12 @@ int eg_sync(eg_graph* g);
 int eg_load_edges(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int symmetric,
                   int where);
 
+/* The same from a binary edge file (the reference's input format, read whole as preload_graph_file
+ * does for one rank, core/graph.hpp:1011-1084): 64 MiB pieces are read into pinned staging buffers
+ * while the previous piece is copied to the device.  The file size must be a multiple of
+ * edge_bytes. */
+int eg_load_file(eg_graph* g, const char* path, uint32_t V, int edge_bytes, int symmetric);
+
 /* ---- preprocessing: split_graph core/graph.hpp:981-1009 ---------------------------------- */
 /* Degree histogram, CPBT partition (assign_vertices :662-792, dense out-degree weights with
  * T = max_iterations), then the CSR (:1248-1355) and/or CSC (:1098-1242). */

@@ -144,3 +144,33 @@ def test_bounded_wait_runs_out_and_handle_survives(eg_lib):
         g.load_directed(eg.pack_edges(src, dst), 4)
         lv, _ = g.bfs(0)
         assert list(lv) == [0, 1, 2, 3]
+
+
+def test_file_ingest_matches_memory_load(eg_lib, tmp_path):
+    """eg_load_file (pieces read into pinned buffers while the previous piece is copied) loads the
+    same graph as eg_load_edges from memory; sizes that are not a multiple of the record size and
+    missing files are rejected."""
+    import endgraph_gb300 as eg
+    rng = np.random.default_rng(21)
+    V, E = 50_000, 9_000_000  # 72 MB of 8-byte records: two staging pieces
+    src = rng.integers(0, V, E).astype(np.uint32)
+    dst = rng.integers(0, V, E).astype(np.uint32)
+    w = rng.random(E).astype(np.float32)
+    for weighted in (False, True):
+        rec = eg.pack_edges(src, dst, w if weighted else None)
+        f = tmp_path / f"g{int(weighted)}.bin"
+        rec.tofile(f)
+        with eg.Graph() as a, eg.Graph() as b:
+            a.load_file(str(f), V, rec.shape[1] * 4)
+            a.build()
+            b.load_directed(rec, V)
+            ca, cb = a.csr(), b.csr()
+            assert lists_equal(ca["off"][0], ca["adj"], cb["off"][0], cb["adj"], ca["w"], cb["w"])
+            assert np.array_equal(a.partition()[0], b.partition()[0])
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(b"\0" * 20)
+    with eg.Graph() as g:
+        with pytest.raises(eg.EndGraphError):
+            g.load_file(str(bad), 10, 8)
+        with pytest.raises(eg.EndGraphError):
+            g.load_file(str(tmp_path / "missing.bin"), 10, 8)
