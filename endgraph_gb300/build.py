@@ -92,6 +92,17 @@ def build_toolkits() -> str:
         link = os.path.join(TOOLKIT_DIR, t)
         if not os.path.lexists(link):
             os.symlink("eg_toolkit", link)
+    # betweenness centrality: device operators on the engine API, compiled with nvcc
+    bc_src = os.path.join(os.path.dirname(TOOLKIT_SRC), "bc.cu")
+    bc_exe = os.path.join(TOOLKIT_DIR, "bc")
+    bc_deps = [bc_src, lib] + glob.glob(os.path.join(INCLUDE, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "core", "*.hpp"))
+    if not os.path.exists(bc_exe) or os.path.getmtime(bc_exe) < max(os.path.getmtime(p) for p in bc_deps):
+        cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "--expt-relaxed-constexpr", f"-I{INCLUDE}", bc_src, "-o",
+               bc_exe + ".tmp", f"-L{HERE}", "-lendgraph_gb300", "-Xlinker", f"-rpath={HERE}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"bc toolkit build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(bc_exe + ".tmp", bc_exe)
     return TOOLKIT_DIR
 
 

@@ -239,6 +239,26 @@ static __global__ void k_fill_words(unsigned long long* words, uint64_t nwords, 
     }
 }
 
+// ordered compaction of the vertices with out-edges into a compressed index over the CSR (the
+// pull side of the transposed graph), closed by a {V, E} sentinel
+struct LoadHasOut {
+    const uint32_t* deg;
+    uint32_t V;
+    __device__ uint32_t operator()(uint64_t i) const { return i >= V ? 1u : (deg[i] > 0 ? 1u : 0u); }
+};
+struct EpiRowIndex {
+    const uint64_t* off;
+    uint32_t V;
+    uint64_t E;
+    uint32_t* cvert;
+    uint64_t* cidx;
+    __device__ void operator()(uint64_t i, uint64_t excl, uint32_t flag) const {
+        if (!flag) return;
+        cvert[excl] = i >= V ? V : (uint32_t)i;
+        cidx[excl] = i >= V ? E : off[i];
+    }
+};
+
 }  // namespace detail
 
 // One engine per built graph.  All work is ordered on the graph handle's stream; the results of
@@ -252,7 +272,6 @@ class Engine {
         V_ = info.V;
         E_ = info.E;
         P_ = (int)info.partitions;
-        nitems_ = info.ncompressed - 1;
         check_eg(eg_get_csr(g, &csr_), "eg_get_csr");
         check_eg(eg_get_csc(g, &csc_), "eg_get_csc");
         stream_ = (cudaStream_t)eg_stream(g);
@@ -267,22 +286,29 @@ class Engine {
         q1_ = alloc<uint32_t>((size_t)V_ + 1);
         ipref_ = alloc<uint64_t>((size_t)V_ * P_ + 2);
         push_chunk_ = alloc<uint32_t>(E_ / kPushChunk + 4);
-        scan_desc_ = alloc<uint64_t>(((size_t)V_ * P_ + kScanTile) / kScanTile + 1);
-        // pull chunks: first compressed entry per 4096-edge chunk and the entries crossing chunks
-        nchunks_ = (E_ + kPullChunk - 1) / kPullChunk;
-        pull_chunk_ = alloc<uint32_t>(nchunks_ + 2);
-        split_ = alloc<uint32_t>(nchunks_ + 2);
-        check(cudaMemsetAsync(counters_, 0, 64, stream_), "cudaMemsetAsync");
-        k_pull_chunks<<<grid(nitems_), 256, 0, stream_>>>(csc_.cidx, csc_.cvert, nitems_, nchunks_, pull_chunk_, split_,
-                                                         counters_);
-        check(cudaGetLastError(), "k_pull_chunks");
-        check(cudaMemcpyAsync(&nsplit_, counters_, 8, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
-        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        scan_desc_ = alloc<uint64_t>(((size_t)V_ * P_ + kScanTile) / kScanTile + 2);
+        // as built: push along the CSR, pull over the compressed CSC
+        Side& f = side_[0];
+        f.push_off = csr_.off;
+        f.push_adj = csr_.adj;
+        f.push_w = csr_.w;
+        f.push_deg = outdeg_;
+        f.pull_adj = csc_.adj;
+        f.pull_w = csc_.w;
+        f.pull_cvert = csc_.cvert;
+        f.pull_cidx = csc_.cidx;
+        f.pull_deg = indeg_;
+        f.nitems = info.ncompressed - 1;
+        setup_pull_chunks(f);
+        cur_ = &side_[0];
     }
     ~Engine() {
         for (void* p : {(void*)outdeg_, (void*)indeg_, (void*)counters_, (void*)q0_, (void*)q1_, (void*)ipref_,
-                        (void*)push_chunk_, (void*)scan_desc_, (void*)pull_chunk_, (void*)split_, msg_, partial_})
+                        (void*)push_chunk_, (void*)scan_desc_, msg_, partial_, (void*)row_cvert_, (void*)row_cidx_})
             if (p) cudaFree(p);
+        for (Side& sd : side_)
+            for (void* p : {(void*)sd.chunk, (void*)sd.split})
+                if (p) cudaFree(p);
     }
     Engine(const Engine&) = delete;
     Engine& operator=(const Engine&) = delete;
@@ -293,6 +319,18 @@ class Engine {
     const uint32_t* out_degree() const { return outdeg_; }  // device
     const uint32_t* in_degree() const { return indeg_; }    // device
     bool last_was_dense() const { return last_dense_; }
+
+    // process_edges on the transposed graph: push along in-edges (the CSC lists) and pull over
+    // out-edges (the CSR lists, indexed on first use) -- the reverse sweeps of a backward pass
+    // (the reference's transpose(), core/graph.hpp:649-657, swaps the same two structures).
+    // Degrees, the switch's active-edge count and process_edges' roles follow the orientation.
+    // One partition only.
+    void set_transposed(bool t) {
+        if (t && P_ != 1) throw Error(EG_ERR_UNSUPPORTED, "set_transposed: one partition only");
+        if (t && !side_[1].ready) setup_transposed();
+        cur_ = &side_[t ? 1 : 0];
+    }
+    bool transposed() const { return cur_ == &side_[1]; }
     uint64_t last_active_edges() const { return last_active_edges_; }
 
     // vertex arrays and subsets in device memory (alloc_vertex_array / alloc_vertex_subset)
@@ -362,7 +400,7 @@ class Engine {
         if (mode != Mode::Dense) {
             check(cudaMemsetAsync(counters_ + 2, 0, 16, stream_), "cudaMemsetAsync");
             k_bm_compact<<<grid(active.nwords()), 256, 0, stream_>>>(active.words, active.nwords(), q0_, d_n, d_act,
-                                                                     outdeg_);
+                                                                     cur_->push_deg);
             check(cudaGetLastError(), "k_bm_compact");
             struct {
                 uint32_t n, pad;
@@ -422,7 +460,8 @@ class Engine {
         check(cudaMemsetAsync(counters_ + 5, 0, 8, stream_), "cudaMemsetAsync");  // ticket + error flag
         uint32_t* ticket = reinterpret_cast<uint32_t*>(counters_ + 5);
         int* err = reinterpret_cast<int*>(ticket + 1);
-        LoadItemLen ld{q1_, P_, (uint64_t)V_ + 1, csr_.off};
+        const Side& sd = *cur_;
+        LoadItemLen ld{q1_, P_, (uint64_t)V_ + 1, sd.push_off};
         EpiItemRank ep{ipref_, push_chunk_};
         k_scan<<<(unsigned)tiles, kScanThreads, 0, stream_>>>(ld, ep, nitems, scan_desc_, ticket, err, ipref_ + nitems,
                                                              kLookbackSpinCap);
@@ -432,16 +471,16 @@ class Engine {
         a.nitems = nitems;
         a.P = P_;
         a.stride = (uint64_t)V_ + 1;
-        a.off = csr_.off;
-        a.adj = csr_.adj;
-        a.w = csr_.w;
+        a.off = sd.push_off;
+        a.adj = sd.push_adj;
+        a.w = sd.push_w;
         a.ipref = ipref_;
         a.chunk_item = push_chunk_;
         a.q_out = nullptr;
         a.n_out = nullptr;
         a.act_edges = nullptr;
         a.deg = nullptr;
-        detail::PushAdapter<Op> pa{op, msg, csr_.w, out};
+        detail::PushAdapter<Op> pa{op, msg, sd.push_w, out};
         k_push<detail::PushAdapter<Op>><<<(unsigned)num_sms_ * 8u, kPushThreads, 0, stream_>>>(pa, a);
         check(cudaGetLastError(), "k_push");
         int h_err = 0;
@@ -453,7 +492,8 @@ class Engine {
     template <class Op>
     void run_dense(const Op& op, typename Op::R* out) {
         using Acc = typename Op::Acc;
-        if (nchunks_ == 0) return;
+        const Side& sd = *cur_;
+        if (sd.nchunks == 0) return;
         // partial reductions start at the operator's identity
         const typename Op::Acc id = host_identity(op);
         unsigned long long id_bits = 0;
@@ -470,23 +510,90 @@ class Engine {
             partial_size_ = sizeof(Acc);
             partial_id_ = id_bits;
         }
-        detail::PullAdapter<Op> pa{op, csc_.w, static_cast<Acc*>(partial_), out, P_ == 1 ? 1 : 0};
+        detail::PullAdapter<Op> pa{op, sd.pull_w, static_cast<Acc*>(partial_), out, P_ == 1 ? 1 : 0};
         using K = detail::PullAdapter<Op>;
         const int cap = (int)kPullChunk + P_ + 2;
         const size_t smem = align16(sizeof(uint32_t) * (cap + 1)) + sizeof(Acc) * cap + cap;
         check(cudaFuncSetAttribute(k_pull<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem");
         int per_sm = 0;
         check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<K>, kPullThreads, smem), "occupancy");
-        const unsigned g = (unsigned)std::min<uint64_t>(nchunks_, (uint64_t)num_sms_ * (uint64_t)std::max(per_sm, 1));
-        k_pull<K><<<g, kPullThreads, smem, stream_>>>(pa, csc_.adj, csc_.cidx, csc_.cvert, pull_chunk_, E_, nitems_,
-                                                     nchunks_, V_, cap);
+        const unsigned g = (unsigned)std::min<uint64_t>(sd.nchunks, (uint64_t)num_sms_ * (uint64_t)std::max(per_sm, 1));
+        k_pull<K><<<g, kPullThreads, smem, stream_>>>(pa, sd.pull_adj, sd.pull_cidx, sd.pull_cvert, sd.chunk, E_,
+                                                     sd.nitems, sd.nchunks, V_, cap);
         check(cudaGetLastError(), "k_pull");
-        const uint64_t n = P_ == 1 ? nsplit_ : V_;
+        const uint64_t n = P_ == 1 ? sd.nsplit : V_;
         if (n)
-            detail::k_dense_finish<Op><<<grid(n), 256, 0, stream_>>>(op, P_ == 1 ? split_ : nullptr, csc_.cvert,
-                                                                    nsplit_, indeg_, V_, static_cast<Acc*>(partial_),
-                                                                    out);
+            detail::k_dense_finish<Op><<<grid(n), 256, 0, stream_>>>(op, P_ == 1 ? sd.split : nullptr, sd.pull_cvert,
+                                                                    sd.nsplit, sd.pull_deg, V_,
+                                                                    static_cast<Acc*>(partial_), out);
         check(cudaGetLastError(), "k_dense_finish");
+    }
+
+    struct Side {
+        const uint64_t* push_off = nullptr;  // [P*(V+1)] list offsets of the push direction
+        const uint32_t* push_adj = nullptr;
+        const float* push_w = nullptr;
+        const uint32_t* push_deg = nullptr;  // list lengths (active-edge count of the switch)
+        const uint32_t* pull_adj = nullptr;
+        const float* pull_w = nullptr;
+        const uint32_t* pull_cvert = nullptr;  // compressed index of the pull direction
+        const uint64_t* pull_cidx = nullptr;
+        const uint32_t* pull_deg = nullptr;
+        uint64_t nitems = 0, nchunks = 0;
+        uint32_t* chunk = nullptr;  // first compressed entry per 4096-edge chunk
+        uint32_t* split = nullptr;  // entries whose list crosses a chunk boundary
+        unsigned long long nsplit = 0;
+        bool ready = false;
+    };
+
+    void setup_pull_chunks(Side& sd) {
+        sd.nchunks = (E_ + kPullChunk - 1) / kPullChunk;
+        sd.chunk = alloc<uint32_t>(sd.nchunks + 2);
+        sd.split = alloc<uint32_t>(sd.nchunks + 2);
+        check(cudaMemsetAsync(counters_, 0, 64, stream_), "cudaMemsetAsync");
+        k_pull_chunks<<<grid(sd.nitems), 256, 0, stream_>>>(sd.pull_cidx, sd.pull_cvert, sd.nitems, sd.nchunks, sd.chunk,
+                                                           sd.split, counters_);
+        check(cudaGetLastError(), "k_pull_chunks");
+        check(cudaMemcpyAsync(&sd.nsplit, counters_, 8, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        sd.ready = true;
+    }
+
+    void setup_transposed() {
+        Side& b = side_[1];
+        b.push_off = csc_.off;
+        b.push_adj = csc_.adj;
+        b.push_w = csc_.w;
+        b.push_deg = indeg_;
+        b.pull_adj = csr_.adj;
+        b.pull_w = csr_.w;
+        b.pull_deg = outdeg_;
+        // compressed index over the CSR: one {vertex, start} per vertex with out-edges + {V, E}
+        row_cvert_ = alloc<uint32_t>((size_t)V_ + 1);
+        row_cidx_ = alloc<uint64_t>((size_t)V_ + 1);
+        const uint64_t n = (uint64_t)V_ + 1;
+        const uint64_t tiles = (n + kScanTile - 1) / kScanTile;
+        uint64_t* desc = alloc<uint64_t>(tiles);
+        check(cudaMemsetAsync(desc, 0, 8 * tiles, stream_), "cudaMemsetAsync");
+        check(cudaMemsetAsync(counters_ + 5, 0, 8, stream_), "cudaMemsetAsync");
+        uint32_t* ticket = reinterpret_cast<uint32_t*>(counters_ + 5);
+        uint64_t* total = reinterpret_cast<uint64_t*>(counters_ + 4);
+        k_scan<<<(unsigned)tiles, kScanThreads, 0, stream_>>>(detail::LoadHasOut{outdeg_, V_},
+                                                               detail::EpiRowIndex{csr_.off, V_, E_, row_cvert_, row_cidx_},
+                                                               n, desc, ticket, reinterpret_cast<int*>(ticket + 1), total,
+                                                               kLookbackSpinCap);
+        check(cudaGetLastError(), "k_scan");
+        unsigned long long nc = 0;
+        int err = 0;
+        check(cudaMemcpyAsync(&nc, total, 8, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaMemcpyAsync(&err, ticket + 1, 4, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        cudaFree(desc);
+        if (err) throw Error(EG_ERR_TIMEOUT, "set_transposed: a bounded device wait gave up");
+        b.pull_cvert = row_cvert_;
+        b.pull_cidx = row_cidx_;
+        b.nitems = nc - 1;  // the sentinel closes the last list
+        setup_pull_chunks(b);
     }
 
     // the identity is a device function; evaluate it once on the device
@@ -506,7 +613,6 @@ class Engine {
     uint32_t V_ = 0;
     uint64_t E_ = 0;
     int P_ = 1;
-    uint64_t nitems_ = 0;
     eg_csr_view csr_{};
     eg_csc_view csc_{};
     cudaStream_t stream_ = nullptr;
@@ -519,10 +625,10 @@ class Engine {
     uint64_t* ipref_ = nullptr;
     uint32_t* push_chunk_ = nullptr;
     uint64_t* scan_desc_ = nullptr;
-    uint64_t nchunks_ = 0;
-    uint32_t* pull_chunk_ = nullptr;
-    uint32_t* split_ = nullptr;
-    unsigned long long nsplit_ = 0;
+    Side side_[2];  // as built, transposed
+    Side* cur_ = nullptr;
+    uint32_t* row_cvert_ = nullptr;
+    uint64_t* row_cidx_ = nullptr;
     void* msg_ = nullptr;
     size_t msg_bytes_ = 0;
     void* partial_ = nullptr;

@@ -95,6 +95,7 @@ def lib():
         L.ora_bfs_check_parents.restype = ctypes.c_uint64
         L.ora_cc_labels.argtypes = [_u32p, _u32p, ctypes.c_uint64, ctypes.c_uint32, _u32p]
         L.ora_sssp.argtypes = [_u64p, _u32p, _f32p, ctypes.c_uint32, ctypes.c_uint32, _f32p]
+        L.ora_bc.argtypes = [_u64p, _u32p, ctypes.c_uint32, ctypes.c_uint32, _f64p, _f64p, _u32p]
         L.ora_adjacency_hash.argtypes = [_u32p, _u32p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                          _u64p, _u64p]
         _lib = L
@@ -180,6 +181,15 @@ def pagerank(csc_off, csc_src, outdeg, V, iterations=20, damping=0.85):
     out = np.empty(max(V, 1), np.float64)
     lib().ora_pagerank(np.ascontiguousarray(csc_off, np.uint64), csc_src, outdeg, V, iterations, damping, out)
     return out[:V]
+
+
+def bc(csr_off, csr_dst, V, root):
+    """(sigma, delta, level) of single-source betweenness from root (Brandes)."""
+    sigma = np.empty(V, np.float64)
+    delta = np.empty(V, np.float64)
+    level = np.empty(V, np.uint32)
+    lib().ora_bc(np.ascontiguousarray(csr_off, np.uint64), csr_dst, V, root, sigma, delta, level)
+    return sigma, delta, level
 
 
 def bfs_levels(csr_off, csr_dst, V, root):

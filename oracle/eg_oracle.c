@@ -334,6 +334,39 @@ void ora_sssp(const uint64_t* off, const uint32_t* adj, const float* w, uint32_t
     free(h);
 }
 
+void ora_bc(const uint64_t* off, const uint32_t* adj, uint32_t V, uint32_t root, double* sigma, double* delta,
+            uint32_t* level) {
+    uint32_t* order = (uint32_t*)malloc(sizeof(uint32_t) * (V ? V : 1));
+    for (uint32_t v = 0; v < V; ++v) {
+        sigma[v] = 0.0;
+        delta[v] = 0.0;
+        level[v] = ORA_UNREACHED;
+    }
+    uint32_t head = 0, tail = 0;
+    sigma[root] = 1.0;
+    level[root] = 0;
+    order[tail++] = root;
+    while (head < tail) {
+        const uint32_t v = order[head++];
+        for (uint64_t e = off[v]; e < off[v + 1]; ++e) {
+            const uint32_t w = adj[e];
+            if (level[w] == ORA_UNREACHED) {
+                level[w] = level[v] + 1;
+                order[tail++] = w;
+            }
+            if (level[w] == level[v] + 1) sigma[w] += sigma[v];
+        }
+    }
+    for (uint32_t i = tail; i-- > 0;) {
+        const uint32_t w = order[i];
+        for (uint64_t e = off[w]; e < off[w + 1]; ++e) {
+            const uint32_t x = adj[e];
+            if (level[x] == level[w] + 1) delta[w] += sigma[w] / sigma[x] * (1.0 + delta[x]);
+        }
+    }
+    free(order);
+}
+
 void ora_adjacency_hash(const uint32_t* src, const uint32_t* dst, const float* w, uint64_t E, uint32_t V,
                         uint64_t* hout, uint64_t* hin) {
     memset(hout, 0, sizeof(uint64_t) * V);

@@ -86,6 +86,13 @@ void ora_cc_labels(const uint32_t* src, const uint32_t* dst, uint64_t E, uint32_
 void ora_sssp(const uint64_t* csr_off, const uint32_t* csr_dst, const float* csr_w, uint32_t V,
               uint32_t root, float* dist);
 
+/* Single-source betweenness dependencies (Brandes 2001; BC is named by the reference README,
+ * README.md:24,37, without code in its tree): BFS over out-edges counting shortest paths sigma,
+ * then delta[v] = sum over out-neighbours w one level deeper of sigma[v]/sigma[w]*(1+delta[w]),
+ * accumulated in reverse BFS order.  level: BFS level, ORA_UNREACHED when unreached. */
+void ora_bc(const uint64_t* csr_off, const uint32_t* csr_dst, uint32_t V, uint32_t root, double* sigma,
+            double* delta, uint32_t* level);
+
 /* Order-independent per-vertex neighbour signatures: hout[s] += mix(d | wbits<<32),
  * hin[d] += mix(s | wbits<<32) (wbits = 0 when w is NULL). */
 void ora_adjacency_hash(const uint32_t* src, const uint32_t* dst, const float* w, uint64_t E, uint32_t V,
