@@ -408,6 +408,8 @@ __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_
     const uint64_t e0 = blockIdx.x * chunk;
     const uint64_t e1 = e0 + chunk < E ? e0 + chunk : E;
     constexpr int kPer = scatter_per(REC);
+    unsigned long long keep;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(keep));
     for (uint64_t t0 = e0; t0 < e1; t0 += scatter_tile(REC)) {
         uint32_t rec[kPer][W];
         bool valid[kPer];
@@ -451,8 +453,12 @@ __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_
                 const uint32_t b = r[half] >> shift;
                 const uint64_t pos = base[b] + (i - s_cnt[b]);
                 uint32_t* o = reinterpret_cast<uint32_t*>(out + pos * REC);
-                if (W == 2) {  // 8-byte records: one 8-byte store
-                    *reinterpret_cast<uint2*>(o) = *reinterpret_cast<const uint2*>(r);
+                if (W == 2) {  // 8-byte records: one 8-byte store, kept in L2 (the next tile's run
+                               // of the same bucket completes its partial sectors)
+                    const uint2 q = *reinterpret_cast<const uint2*>(r);
+                    asm volatile("st.global.L2::cache_hint.v2.u32 [%0], {%1, %2}, %3;" ::"l"(o), "r"(q.x), "r"(q.y),
+                                 "l"(keep)
+                                 : "memory");
                 } else {
 #pragma unroll
                     for (int w = 0; w < W; ++w) o[w] = r[w];
@@ -513,6 +519,10 @@ __device__ __forceinline__ void for_records(const uint8_t* __restrict__ rec, uin
     }
 }
 
+__device__ __forceinline__ void st_keep_u32(uint32_t* p, uint32_t v, unsigned long long policy) {
+    asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(policy) : "memory");
+}
+
 // C: one bucket per CTA iteration (persistent CTAs take buckets from a ticket)
 template <int REC>
 __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* __restrict__ rec, const uint64_t* __restrict__ excl,
@@ -522,6 +532,10 @@ __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* _
                                                                  uint32_t* __restrict__ adj, float* __restrict__ wout,
                                                                  uint32_t* ticket, int vec_ok) {
     const bool vec = vec_ok != 0;
+    // the 4-byte placement stores land at random positions of the bucket's window: ask L2 to keep
+    // those lines so that a partly written sector is usually completed before it is evicted
+    unsigned long long keep;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(keep));
     extern __shared__ uint32_t s_cnt[];  // LB counters
     __shared__ uint32_t s_warp[32];
     __shared__ uint32_t s_b;
@@ -549,8 +563,8 @@ __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* _
         __syncthreads();
         for_records<REC>(rec, r0, r1, vec, [&](uint32_t s, uint32_t d, uint32_t wb) {
             const uint64_t pos = r0 + atomicAdd(&s_cnt[(key_is_src ? s : d) - v0], 1u);
-            adj[pos] = key_is_src ? d : s;
-            if (REC == 12) wout[pos] = __uint_as_float(wb);
+            st_keep_u32(adj + pos, key_is_src ? d : s, keep);
+            if (REC == 12) st_keep_u32(reinterpret_cast<uint32_t*>(wout) + pos, wb, keep);
         });
         __syncthreads();
     }
