@@ -62,7 +62,7 @@ struct MsBfsPullOp {  // k_pull_direct operator
     __device__ Acc combine(Acc a, Acc b) const { return a | b; }
     __device__ Acc gather(uint32_t u) const {
         if (screen && !bm_has(front_bm, u)) return 0ull;
-        return __ldcg(front + u);
+        return ld_keep(front + u);
     }
     __device__ __forceinline__ void finish_direct(uint32_t v, Acc m) const {
         const unsigned long long fresh = m & ~__ldcg(visit + v);
@@ -930,7 +930,7 @@ struct PprPullOp {
     float* acc;
     float scale;
     __device__ Acc identity() const { return 0.f; }
-    __device__ Acc gather(uint32_t u, uint64_t e) const { return __ldcg(x + u) * __ldg(wn + e); }
+    __device__ Acc gather(uint32_t u, uint64_t e) const { return ld_keep(x + u) * __ldg(wn + e); }
     __device__ Acc combine(Acc a, Acc b) const { return a + b; }
     __device__ void smem_add(Acc* slot, Acc v) const { atomicAdd(slot, v); }
     __device__ void finish(bool ok, uint32_t v, Acc a, bool whole) const {

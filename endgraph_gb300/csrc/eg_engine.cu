@@ -261,7 +261,7 @@ struct PrPullOp {  // toolkits/pagerank.cpp:64-97: sum curr[src]; next = 1-d+d*s
     float base, d;
     int divide, single;
     __device__ Acc identity() const { return 0.f; }
-    __device__ Acc gather(uint32_t src, uint64_t) const { return __ldcg(curr + src); }
+    __device__ Acc gather(uint32_t src, uint64_t) const { return ld_keep(curr + src); }
     __device__ Acc combine(Acc a, Acc b) const { return a + b; }
     __device__ void smem_add(Acc* slot, Acc v) const { atomicAdd(slot, v); }
     __device__ void finish(bool ok, uint32_t v, Acc a, bool whole) const {
@@ -291,7 +291,7 @@ struct CcPullOp {  // toolkits/cc.cpp:62-80: min label over in-neighbours, write
     unsigned long long* act_edges;
     const uint32_t* deg;
     __device__ Acc identity() const { return 0xFFFFFFFFu; }
-    __device__ Acc gather(uint32_t src, uint64_t) const { return __ldcg(label + src); }
+    __device__ Acc gather(uint32_t src, uint64_t) const { return ld_keep(label + src); }
     __device__ Acc combine(Acc a, Acc b) const { return a < b ? a : b; }
     __device__ void smem_add(Acc* slot, Acc v) const { atomicMin(slot, v); }
     __device__ void finish(bool ok, uint32_t v, Acc m, bool) const {

@@ -29,6 +29,30 @@ namespace eg {
 // shared-memory sub-arrays start on 16-byte boundaries (vector and 8-byte accesses)
 __host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
+// Gathers from a vertex array (ranks, labels, frontier words) ask L2 to keep half of what they
+// touch ahead of the streamed adjacency: a 128 MiB rank array then stays mostly resident.
+// Loads are L2-coherent (.cg), like __ldcg.
+__device__ __forceinline__ unsigned long long l2_keep_policy() {
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 0.5;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ float ld_keep(const float* a) {
+    float v;
+    asm volatile("ld.global.cg.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(l2_keep_policy()));
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_keep(const uint32_t* a) {
+    uint32_t v;
+    asm volatile("ld.global.cg.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(l2_keep_policy()));
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_keep(const unsigned long long* a) {
+    unsigned long long v;
+    asm volatile("ld.global.cg.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(a), "l"(l2_keep_policy()));
+    return v;
+}
+
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
