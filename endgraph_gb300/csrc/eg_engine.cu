@@ -80,9 +80,12 @@ __device__ __forceinline__ bool bu_claim(const BuArgs& a, uint32_t v, uint32_t p
 }
 
 __global__ void __launch_bounds__(256) k_bu_head(BuArgs a) {
+    __shared__ uint32_t s_cnt[2 * (256 / 32 + 1)];
     const int lane = threadIdx.x & 31;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.nitems; base += stride) {
+    unsigned long long my_act = 0;  // out-edges of the vertices this thread activated
+    int parity = 0;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.nitems; base += stride, parity ^= 1) {
         const uint64_t i = base + threadIdx.x;
         bool act = false;
         uint32_t v = a.V, nsg = 0;
@@ -108,7 +111,8 @@ __global__ void __launch_bounds__(256) k_bu_head(BuArgs a) {
                 else if (e > h) nsg = (uint32_t)((e - h + kBuSeg - 1) / kBuSeg);
             }
         }
-        append_active(act, v, a.q_out, a.n_out, a.act_edges, a.deg);
+        append_block(act, v, a.q_out, a.n_out, s_cnt, parity);
+        if (act) my_act += a.deg[v];
         uint32_t incl = nsg;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -123,6 +127,9 @@ __global__ void __launch_bounds__(256) k_bu_head(BuArgs a) {
             for (uint32_t k = 0; k < nsg; ++k) a.seg[at + k] = ((unsigned long long)k << 32) | (uint32_t)i;
         }
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) my_act += __shfl_xor_sync(0xffffffffu, my_act, o);
+    if (lane == 0 && my_act) atomicAdd(a.act_edges, my_act);
 }
 
 __global__ void __launch_bounds__(256) k_bu_tail(BuArgs a) {

@@ -452,6 +452,30 @@ __device__ __forceinline__ void append_active(bool act, uint32_t w, uint32_t* q_
     }
 }
 
+// CTA-aggregated append for loops that are uniform across the CTA: one global atomic per CTA
+// step instead of one per warp (a single queue counter takes every step's activations).
+// s_cnt: 2 * (warps + 1) shared words; parity alternates between steps so that one barrier
+// pair per step suffices.
+__device__ __forceinline__ void append_block(bool act, uint32_t w, uint32_t* q_out, uint32_t* n_out, uint32_t* s_cnt,
+                                             int parity) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t* c = s_cnt + parity * (nw + 1);
+    const unsigned mask = __ballot_sync(0xffffffffu, act);
+    if (lane == 0) c[warp] = (uint32_t)__popc(mask);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int i = 0; i < nw; ++i) {
+            const uint32_t x = c[i];
+            c[i] = t;
+            t += x;
+        }
+        c[nw] = t ? atomicAdd(n_out, t) : 0u;
+    }
+    __syncthreads();
+    if (act) q_out[c[nw] + c[warp] + (uint32_t)__popc(mask & ((1u << lane) - 1u))] = w;
+}
+
 // push expansion over the frontier items (vertex q[i / P], partition i % P)
 struct PushArgs {
     const uint32_t* q;
@@ -486,9 +510,13 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Op op, PushArgs a) {
     using Val = typename push_value<Op>::type;
     constexpr bool kReduce = !std::is_void<Val>::value;
     std::conditional_t<kReduce, Val, int> acc{};
+    __shared__ uint32_t s_cnt[kPushThreads / 32 + 1];
+    unsigned long long my_act = 0;  // out-edges of the vertices this thread activated
     const uint64_t T = a.ipref[a.nitems];
     const uint64_t nchunks = (T + kPushChunk - 1) / kPushChunk;
     for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        uint32_t got[kPushPerThread];  // activated vertices of this thread's edges (slot q: edge q)
+        uint32_t got_mask = 0;
         const uint64_t e0 = c * kPushChunk;
         const uint64_t e1 = e0 + kPushChunk < T ? e0 + kPushChunk : T;
         const uint64_t eb = e0 + (uint64_t)threadIdx.x * kPushPerThread;
@@ -526,8 +554,46 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Op op, PushArgs a) {
                 if constexpr (kReduce) act = op.relax(u, pay, wv, pos, acc);
                 else act = op.relax(u, pay, wv, pos);
             }
-            append_active(act, wv, a.q_out, a.n_out, a.act_edges, a.deg);
+            got[q] = wv;
+            if (act) got_mask |= 1u << q;
         }
+        // one queue reservation per CTA and chunk (a single counter takes every activation)
+        if (a.q_out) {
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kPushThreads / 32;
+            const uint32_t cnt = (uint32_t)__popc(got_mask);
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) s_cnt[warp] = incl;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t t = 0;
+                for (int i = 0; i < nw; ++i) {
+                    const uint32_t x = s_cnt[i];
+                    s_cnt[i] = t;
+                    t += x;
+                }
+                s_cnt[nw] = t ? atomicAdd(a.n_out, t) : 0u;
+            }
+            __syncthreads();
+            uint32_t at = s_cnt[nw] + s_cnt[warp] + incl - cnt;
+#pragma unroll
+            for (int q = 0; q < kPushPerThread; ++q) {
+                if ((got_mask >> q) & 1u) {
+                    a.q_out[at++] = got[q];
+                    if (a.act_edges) my_act += a.deg[got[q]];
+                }
+            }
+            __syncthreads();  // s_cnt is reused by the next chunk
+        }
+    }
+    if (a.act_edges) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) my_act += __shfl_xor_sync(0xffffffffu, my_act, o);
+        if ((threadIdx.x & 31) == 0 && my_act) atomicAdd(a.act_edges, my_act);
     }
     if constexpr (kReduce) {
 #pragma unroll
