@@ -72,6 +72,109 @@ struct MsBfsPullOp {  // k_pull_direct operator
     }
 };
 
+// Early-exit dense level: a destination stops reading in-edges as soon as its visited word holds
+// every root still running (nothing more can reach it in this level).  One thread per compressed
+// entry reads the first kMsHead in-edges; longer lists continue as kMsSeg-edge segments, one warp
+// each, that apply their partial OR every 128 edges so that other segments of the same
+// destination see the coverage.  Partial ORs are applied like finish_direct (idempotent).
+constexpr uint32_t kMsHead = 8;
+constexpr uint32_t kMsSeg = 1024;
+
+struct MsBuArgs {
+    const uint32_t* adj;
+    const uint64_t* cidx;
+    const uint32_t* cvert;
+    uint64_t nitems;
+    uint32_t V;
+    const unsigned long long* front;
+    unsigned long long* visit;
+    unsigned long long* next;
+    unsigned long long* next_bm;
+    const unsigned long long* alive;
+    unsigned long long* seg;  // (segment << 32) | compressed entry
+    uint32_t* nseg;
+    const int* stop;  // captured level loops: set once a level found nothing new
+};
+
+__device__ __forceinline__ void ms_apply(const MsBuArgs& a, uint32_t v, unsigned long long m) {
+    const unsigned long long fresh = m & ~__ldcg(a.visit + v);
+    if (!fresh) return;
+    const unsigned long long nb = fresh & ~atomicOr(a.visit + v, fresh);
+    if (nb && atomicOr(a.next + v, nb) == 0ull) atomicOr(a.next_bm + (v >> 6), 1ull << (v & 63));
+}
+
+__global__ void __launch_bounds__(256) k_ms_head(MsBuArgs a) {
+    if (a.stop && *(volatile const int*)a.stop) return;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long al = __ldg(a.alive);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < a.nitems; base += stride) {
+        const uint64_t i = base + threadIdx.x;
+        uint32_t nsg = 0;
+        if (i < a.nitems) {
+            const uint32_t v = a.cvert[i];
+            const unsigned long long need = v < a.V ? al & ~__ldcg(a.visit + v) : 0ull;
+            if (need) {
+                const uint64_t s = a.cidx[i], e = a.cidx[i + 1];
+                const uint64_t h = e - s > kMsHead ? s + kMsHead : e;
+                unsigned long long acc = 0;
+                for (uint64_t p = s; p < h && (acc & need) != need; p += 4) {
+                    uint32_t u[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) u[q] = p + q < h ? __ldg(a.adj + p + q) : a.V;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        if (u[q] < a.V) acc |= ld_keep(a.front + u[q]);
+                }
+                if (acc & need) ms_apply(a, v, acc);
+                if ((acc & need) != need && e > h) nsg = (uint32_t)((e - h + kMsSeg - 1) / kMsSeg);
+            }
+        }
+        uint32_t incl = nsg;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+        if (tot) {
+            uint32_t at = 0;
+            if (lane == 31) at = atomicAdd(a.nseg, tot);
+            at = __shfl_sync(0xffffffffu, at, 31) + incl - nsg;
+            for (uint32_t k = 0; k < nsg; ++k) a.seg[at + k] = ((unsigned long long)k << 32) | (uint32_t)i;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_ms_tail(MsBuArgs a) {
+    if (a.stop && *(volatile const int*)a.stop) return;
+    const uint32_t n = __ldcg(a.nseg);
+    const int lane = threadIdx.x & 31;
+    const unsigned long long al = __ldg(a.alive);
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < n; t += nwarps) {
+        const unsigned long long ent = a.seg[t];
+        const uint32_t i = (uint32_t)ent;
+        const uint32_t v = a.cvert[i];
+        const uint64_t e = a.cidx[i + 1];
+        uint64_t p = a.cidx[i] + kMsHead + (ent >> 32) * kMsSeg;
+        const uint64_t pe = p + kMsSeg < e ? p + kMsSeg : e;
+        for (; p < pe; p += 128) {
+            const unsigned long long vis = __shfl_sync(0xffffffffu, __ldcg(a.visit + v), 0);
+            if ((vis & al) == al) break;  // every running root already reached v
+            unsigned long long acc = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint64_t x = p + 32 * q + lane;
+                if (x < pe) acc |= ld_keep(a.front + __ldg(a.adj + x));
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc |= __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0 && (acc & ~vis)) ms_apply(a, v, acc);
+        }
+    }
+}
+
 struct MsBfsPushOp {
     const unsigned long long* front;
     unsigned long long* visit;
@@ -493,7 +596,7 @@ int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E) {
 // ---------------------------------------------------------------------------------------------
 struct BatchState {
     DevBuf a64, b64, c64, lev, rows0, rows1, heavy, tmp_out, seeds, wn_csc, wn_csr, s_out, gA, row_of, ck, seg;
-    DevBuf ch0, ch1, flag, level_cnt, entries, n_entries, bm0, bm1, alive;
+    DevBuf ch0, ch1, flag, level_cnt, entries, n_entries, bm0, bm1, alive, ms_seg;
     RowTasks csc_tasks, csr_tasks;
     bool csc_ready = false, csr_ready = false;
     // captured MS-BFS level loop and the shapes it was captured for
@@ -620,8 +723,11 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
     // one level L: frontier word[L&1] / bm[L&1] / queue[L&1] -> the same of parity (L+1)&1.  The
     // queue length lands in *count; captured loops (stop_flag set) pull every level and keep the
     // alive mask at "all roots".
+    // The first dense level follows the frontier's explosion: most destinations miss most roots and
+    // read all their in-edges, which the balanced chunked sweep (k_pull_direct) does best.  Later
+    // dense levels find most destinations nearly covered and use the early-exit pair.
     auto enqueue_level = [&](uint32_t L, uint64_t n_host, bool dense, bool screen, uint32_t* count, const int* stop_flag,
-                             uint32_t* nout_host, unsigned long long* act_host) -> int {
+                             uint32_t* nout_host, unsigned long long* act_host, bool early_exit) -> int {
         const int c = L & 1, x = c ^ 1;
         EG_CUDA(cudaMemsetAsync(word[x], 0, 8 * V, g->stream));
         EG_CUDA(cudaMemsetAsync(bm[x], 0, bm_bytes, g->stream));
@@ -630,9 +736,22 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         if (dense) {
             EG_CUDA(cudaMemsetAsync(count, 0, 4, g->stream));
             if (!stop_flag) EG_CUDA(cudaMemsetAsync(d_act, 0, 8, g->stream));
-            MsBfsPullOp op{word[c], bm[c], screen ? 1 : 0, visit, word[x], bm[x], stop_flag ? alive + 2 : alive + c,
-                           stop_flag};
-            EG_TRY(launch_pull_direct(g, op, "msbfs_pull"));
+            if (early_exit) {
+                uint32_t* d_nseg = reinterpret_cast<uint32_t*>(cnt + kGraphLevels + 2);
+                EG_CUDA(cudaMemsetAsync(d_nseg, 0, 4, g->stream));
+                MsBuArgs ma{g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(),
+                            g->ncompressed - 1, (uint32_t)V, word[c], visit, word[x], bm[x],
+                            stop_flag ? alive + 2 : alive + c, b.ms_seg.as<unsigned long long>(), d_nseg, stop_flag};
+                Timed t(&g->prof, g->stream, "msbfs_pull");
+                k_ms_head<<<grid_for(ma.nitems, 256, grid), 256, 0, g->stream>>>(ma);
+                EG_CHECK_LAUNCH("k_ms_head");
+                k_ms_tail<<<grid, 256, 0, g->stream>>>(ma);
+                EG_CHECK_LAUNCH("k_ms_tail");
+            } else {
+                MsBfsPullOp op{word[c], bm[c], screen ? 1 : 0, visit, word[x], bm[x],
+                               stop_flag ? alive + 2 : alive + c, stop_flag};
+                EG_TRY(launch_pull_direct(g, op, "msbfs_pull"));
+            }
             Timed t(&g->prof, g->stream, "msbfs_vertex");
             k_bm_compact<<<grid_for(nwords, 256, grid), 256, 0, g->stream>>>(bm[x], nwords, queue[x], count,
                                                                             stop_flag ? nullptr : d_act, deg);
@@ -668,7 +787,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
                     k_level_gate<<<1, 1, 0, g->stream>>>(cnt + L - 1, stop);
                     st = cudaGetLastError() == cudaSuccess ? EG_OK : EG_ERR_CUDA;
                 }
-                if (st == EG_OK) st = enqueue_level(L, 0, true, true, cnt + L, stop, nullptr, nullptr);
+                if (st == EG_OK) st = enqueue_level(L, 0, true, true, cnt + L, stop, nullptr, nullptr, L >= 3);
             }
             cudaGraph_t graph = nullptr;
             cudaError_t e = cudaStreamEndCapture(g->stream, &graph);
@@ -704,7 +823,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
                 set_error("eg_msbfs: more than 254 levels");
                 return EG_ERR_UNSUPPORTED;
             }
-            EG_TRY(enqueue_level(lvl, 0, true, true, d_new, stop, nullptr, nullptr));
+            EG_TRY(enqueue_level(lvl, 0, true, true, d_new, stop, nullptr, nullptr, true));
             ++sweeps;
             uint32_t hn = 0;
             EG_CUDA(cudaMemcpyAsync(&hn, d_new, 4, cudaMemcpyDeviceToHost, g->stream));
@@ -723,6 +842,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         EG_CUDA(cudaStreamSynchronize(g->stream));
         uint64_t n = h.n;
         unsigned long long act = h.act;
+        int dense_levels = 0;
         while (n > 0) {
             if (lvl >= 254) {
                 set_error("eg_msbfs: more than 254 levels");
@@ -732,7 +852,8 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
             const bool dense = !g->built_csr || act >= g->E / (uint64_t)g->dense_div;
             uint32_t nout = 0;
             // a bitmap test before each gather pays only while the frontier is a small part of V
-            EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act));
+            EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act, dense_levels > 0));
+            if (dense) ++dense_levels;
             if (dense) {
                 EG_CUDA(cudaMemcpyAsync(&h, d_nq, 16, cudaMemcpyDeviceToHost, g->stream));
                 EG_CUDA(cudaStreamSynchronize(g->stream));
@@ -771,6 +892,11 @@ static int msbfs_buffers(eg_graph* g, uint32_t n_entries, bool with_levels) {
     EG_TRY(b.bm0.reserve(8 * (V / 64 + 1)));
     EG_TRY(b.bm1.reserve(8 * (V / 64 + 1)));
     EG_TRY(b.alive.reserve(64));
+    {  // early-exit dense levels: at most one segment per entry longer than kMsHead plus one per kMsSeg
+        const uint64_t nitems = g->ncompressed - 1;
+        const uint64_t heavy = std::min<uint64_t>(nitems, g->E / (kMsHead + 1));
+        EG_TRY(b.ms_seg.reserve(sizeof(unsigned long long) * (heavy + g->E / kMsSeg + 2)));
+    }
     EG_TRY(b.entries.reserve(sizeof(uint2) * (n_entries + 1)));
     EG_TRY(b.n_entries.reserve(16));
     if (with_levels) EG_TRY(b.lev.reserve(64 * V + 64));
