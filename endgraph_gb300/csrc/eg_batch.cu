@@ -725,7 +725,10 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
     // alive mask at "all roots".
     // The first dense level follows the frontier's explosion: most destinations miss most roots and
     // read all their in-edges, which the balanced chunked sweep (k_pull_direct) does best.  Later
-    // dense levels find most destinations nearly covered and use the early-exit pair.
+    // dense levels find most destinations nearly covered and use the early-exit pair -- on one
+    // graph.  In a batch of graphs the running-root mask is shared by all graphs, so a vertex
+    // waits for bits its own graph can never deliver, and every level keeps the chunked sweep.
+    const bool one_graph = g->batch_voff.empty();
     auto enqueue_level = [&](uint32_t L, uint64_t n_host, bool dense, bool screen, uint32_t* count, const int* stop_flag,
                              uint32_t* nout_host, unsigned long long* act_host, bool early_exit) -> int {
         const int c = L & 1, x = c ^ 1;
@@ -787,7 +790,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
                     k_level_gate<<<1, 1, 0, g->stream>>>(cnt + L - 1, stop);
                     st = cudaGetLastError() == cudaSuccess ? EG_OK : EG_ERR_CUDA;
                 }
-                if (st == EG_OK) st = enqueue_level(L, 0, true, true, cnt + L, stop, nullptr, nullptr, L >= 3);
+                if (st == EG_OK) st = enqueue_level(L, 0, true, true, cnt + L, stop, nullptr, nullptr, one_graph && L >= 3);
             }
             cudaGraph_t graph = nullptr;
             cudaError_t e = cudaStreamEndCapture(g->stream, &graph);
@@ -823,7 +826,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
                 set_error("eg_msbfs: more than 254 levels");
                 return EG_ERR_UNSUPPORTED;
             }
-            EG_TRY(enqueue_level(lvl, 0, true, true, d_new, stop, nullptr, nullptr, true));
+            EG_TRY(enqueue_level(lvl, 0, true, true, d_new, stop, nullptr, nullptr, one_graph));
             ++sweeps;
             uint32_t hn = 0;
             EG_CUDA(cudaMemcpyAsync(&hn, d_new, 4, cudaMemcpyDeviceToHost, g->stream));
@@ -852,7 +855,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
             const bool dense = !g->built_csr || act >= g->E / (uint64_t)g->dense_div;
             uint32_t nout = 0;
             // a bitmap test before each gather pays only while the frontier is a small part of V
-            EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act, dense_levels > 0));
+            EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act, one_graph && dense_levels > 0));
             if (dense) ++dense_levels;
             if (dense) {
                 EG_CUDA(cudaMemcpyAsync(&h, d_nq, 16, cudaMemcpyDeviceToHost, g->stream));

@@ -310,7 +310,10 @@ struct CcPullOp {  // toolkits/cc.cpp:62-80: min label over in-neighbours, write
                 act = !(atomicOr(next_bm + (v >> 6), bit) & bit);
             }
         }
-        append_active(act, v, q_out, n_out, act_edges, deg);
+        // finish runs in a loop that is uniform across the CTA: one queue reservation per CTA
+        __shared__ uint32_t s_cnt[2 * (kPullThreads / 32 + 1)];
+        __shared__ unsigned long long s_deg[kPullThreads / 32];
+        append_block_deg(act, v, q_out, n_out, act_edges, deg, s_cnt, s_deg, 0);
     }
 };
 

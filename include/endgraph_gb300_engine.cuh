@@ -164,6 +164,7 @@ struct PullAdapter {
 template <class Op>
 __global__ void k_sparse_signal(Op op, const uint32_t* __restrict__ q, const uint32_t* nq, typename Op::Msg* msg,
                                 uint32_t* q_out, uint32_t* n_out) {
+    __shared__ uint32_t s_cnt[2 * (1024 / 32 + 1)];
     const uint32_t n = __ldcg(nq);
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -176,7 +177,7 @@ __global__ void k_sparse_signal(Op op, const uint32_t* __restrict__ q, const uin
             emit = op.sparse_signal(v, m);
             if (emit) msg[v] = m;
         }
-        append_active(emit, v, q_out, n_out, nullptr, nullptr);
+        append_block(emit, v, q_out, n_out, s_cnt, 0);  // the loop is uniform across the CTA
     }
 }
 

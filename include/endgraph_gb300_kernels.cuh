@@ -476,6 +476,38 @@ __device__ __forceinline__ void append_block(bool act, uint32_t w, uint32_t* q_o
     if (act) q_out[c[nw] + c[warp] + (uint32_t)__popc(mask & ((1u << lane) - 1u))] = w;
 }
 
+// The same with the activated vertices' out-degrees summed per CTA into *act_edges.
+// s_cnt: 2 * (warps + 1) words, s_deg: warps words of shared memory.
+__device__ __forceinline__ void append_block_deg(bool act, uint32_t w, uint32_t* q_out, uint32_t* n_out,
+                                                 unsigned long long* act_edges, const uint32_t* deg, uint32_t* s_cnt,
+                                                 unsigned long long* s_deg, int parity) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t* c = s_cnt + parity * (nw + 1);
+    const unsigned mask = __ballot_sync(0xffffffffu, act);
+    unsigned long long d = act ? (unsigned long long)deg[w] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (lane == 0) {
+        c[warp] = (uint32_t)__popc(mask);
+        s_deg[warp] = d;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        unsigned long long dt = 0;
+        for (int i = 0; i < nw; ++i) {
+            const uint32_t x = c[i];
+            c[i] = t;
+            t += x;
+            dt += s_deg[i];
+        }
+        c[nw] = t ? atomicAdd(n_out, t) : 0u;
+        if (dt) atomicAdd(act_edges, dt);
+    }
+    __syncthreads();
+    if (act) q_out[c[nw] + c[warp] + (uint32_t)__popc(mask & ((1u << lane) - 1u))] = w;
+}
+
 // push expansion over the frontier items (vertex q[i / P], partition i % P)
 struct PushArgs {
     const uint32_t* q;
