@@ -230,18 +230,53 @@ __global__ void k_reach_edges(const unsigned long long* __restrict__ visit, cons
     if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
 }
 
-// [V][64] -> [n][V] for the first n columns (32x32 tiles through shared memory)
-__global__ void k_transpose_u8(const uint8_t* __restrict__ in, uint32_t V, int n, uint8_t* __restrict__ out) {
-    __shared__ uint8_t t[64][33];
-    const uint64_t v0 = (uint64_t)blockIdx.x * 32;
-    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
-        const uint64_t v = v0 + i;
-        for (int s = threadIdx.x; s < 64; s += blockDim.x) t[s][i] = v < V ? in[v * 64 + s] : 0;
+// [V][64] level rows -> [n][V] root rows for the first n roots, 64 vertices per CTA: rows come in
+// as 16-byte loads, leave as 16-byte stores of 16 consecutive vertices (vec: V % 16 == 0 and out
+// 16-byte aligned; bytes otherwise).  A byte whose root never reached the vertex (its visited bit
+// is clear) becomes 0xFF, so the level rows need no initialisation.
+__global__ void __launch_bounds__(256) k_levels_out(const uint8_t* __restrict__ lev,
+                                                    const unsigned long long* __restrict__ visit, uint32_t V, int n,
+                                                    uint8_t* __restrict__ out, int vec) {
+    __shared__ __align__(16) uint8_t t[64][68];  // 68-byte rows: column reads spread over banks
+    const uint64_t v0 = (uint64_t)blockIdx.x * 64;
+    {
+        const int r = threadIdx.x >> 2, q = threadIdx.x & 3;
+        const uint64_t v = v0 + r;
+        uint32_t w[4] = {~0u, ~0u, ~0u, ~0u};
+        if (v < V) {
+            const uint4 x = *reinterpret_cast<const uint4*>(lev + v * 64 + 16 * q);
+            const unsigned long long vis = visit[v];
+            w[0] = x.x;
+            w[1] = x.y;
+            w[2] = x.z;
+            w[3] = x.w;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t nib = (uint32_t)(vis >> (16 * q + 4 * j)) & 0xFu;
+                const uint32_t m = ((nib * 0x00204081u) & 0x01010101u) * 0xFFu;  // bit k -> byte k
+                w[j] = (w[j] & m) | ~m;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) *reinterpret_cast<uint32_t*>(&t[r][16 * q + 4 * j]) = w[j];
     }
     __syncthreads();
-    for (int s = threadIdx.y; s < n; s += blockDim.y) {
-        const uint64_t v = v0 + threadIdx.x;
-        if (v < V) out[(uint64_t)s * V + v] = t[s][threadIdx.x];
+    const int s = threadIdx.x >> 2, k = threadIdx.x & 3;
+    if (s >= n) return;
+    const uint64_t vb = v0 + 16 * (uint64_t)k;
+    uint8_t* o = out + (uint64_t)s * V + vb;
+    if (vec && vb + 16 <= V) {
+        uint32_t w[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int b = 16 * k + 4 * j;
+            w[j] = (uint32_t)t[b][s] | ((uint32_t)t[b + 1][s] << 8) | ((uint32_t)t[b + 2][s] << 16) |
+                   ((uint32_t)t[b + 3][s] << 24);
+        }
+        *reinterpret_cast<uint4*>(o) = make_uint4(w[0], w[1], w[2], w[3]);
+    } else {
+        for (int j = 0; j < 16; ++j)
+            if (vb + j < V) o[j] = t[16 * k + j][s];
     }
 }
 
@@ -684,8 +719,10 @@ __global__ void k_level_gate(const uint32_t* prev_new, int* stop) {
 constexpr int kGraphLevels = 32;
 
 // MS-BFS over root entries already in b.entries (count in b.n_entries device word)
+// lev_filled: the level rows start as 0xFF (callers that hand them out as they are); otherwise
+// their unreached bytes are left as they are and masked by k_levels_out
 static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, uint64_t* reach_out, int* sweeps_out,
-                      int* pushes_out) {
+                      int* pushes_out, bool lev_filled) {
     BatchState& b = bstate(g);
     EngineState& s = g->eng;
     const uint64_t V = g->V;
@@ -714,7 +751,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (kGraphLevels + 2), g->stream));
         EG_CUDA(cudaMemcpyAsync(alive + 2, &full, 8, cudaMemcpyHostToDevice, g->stream));
         EG_CUDA(cudaMemcpyAsync(alive, &full, 8, cudaMemcpyHostToDevice, g->stream));
-        if (lev) EG_CUDA(cudaMemsetAsync(lev, 0xFF, 64 * V, g->stream));
+        if (lev && lev_filled) EG_CUDA(cudaMemsetAsync(lev, 0xFF, 64 * V, g->stream));
         k_msbfs_init_entries<<<init_grid, 256, 0, g->stream>>>(b.entries.as<uint2>(), b.n_entries.as<uint32_t>(), visit,
                                                                word[0], bm[0], lev, queue[0], d_nq, d_act, deg);
         EG_CHECK_LAUNCH("k_msbfs_init_entries");
@@ -919,16 +956,20 @@ int run_msbfs(eg_graph* g, const uint32_t* roots, int n, uint8_t* levels, int wh
     uint8_t* lev = levels ? b.lev.as<uint8_t>() : nullptr;
     uint64_t reach = 0;
     int sweeps = 0, pushes = 0;
-    EG_TRY(msbfs_core(g, (uint32_t)n, n, lev, &reach, &sweeps, &pushes));
+    EG_TRY(msbfs_core(g, (uint32_t)n, n, lev, &reach, &sweeps, &pushes, false));
     if (levels) {
         uint8_t* out = levels;
         if (where != EG_DEVICE) {
             EG_TRY(b.tmp_out.reserve((size_t)n * V + 64));
             out = b.tmp_out.as<uint8_t>();
         }
-        dim3 blk(32, 8);
-        k_transpose_u8<<<(unsigned)((V + 31) / 32), blk, 0, g->stream>>>(lev, (uint32_t)V, n, out);
-        EG_CHECK_LAUNCH("k_transpose_u8");
+        {
+            Timed t(&g->prof, g->stream, "msbfs_levels_out");
+            const int vec = (V % 16 == 0) && (((uintptr_t)out & 15u) == 0);
+            k_levels_out<<<(unsigned)((V + 63) / 64), 256, 0, g->stream>>>(lev, b.a64.as<unsigned long long>(),
+                                                                          (uint32_t)V, n, out, vec);
+            EG_CHECK_LAUNCH("k_levels_out");
+        }
         if (where != EG_DEVICE)
             EG_CUDA(cudaMemcpyAsync(levels, out, (size_t)n * V, cudaMemcpyDeviceToHost, g->stream));
     }
@@ -1368,7 +1409,7 @@ int run_msbfs_graphs(eg_graph* g, const uint32_t* roots, int nper, uint8_t* leve
     EG_CUDA(cudaMemcpyAsync(b.n_entries.ptr, &n, 4, cudaMemcpyHostToDevice, g->stream));
     uint64_t reach = 0;
     int sweeps = 0, pushes = 0;
-    EG_TRY(msbfs_core(g, n, nper, levels ? b.lev.as<uint8_t>() : nullptr, &reach, &sweeps, &pushes));
+    EG_TRY(msbfs_core(g, n, nper, levels ? b.lev.as<uint8_t>() : nullptr, &reach, &sweeps, &pushes, true));
     if (levels)
         EG_CUDA(cudaMemcpyAsync(levels, b.lev.ptr, 64ull * g->V,
                                 where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, g->stream));
