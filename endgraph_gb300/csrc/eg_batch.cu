@@ -601,14 +601,6 @@ __global__ void k_fill_f32_rows(float* p, uint64_t n, float v) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) p[i] = v;
 }
 
-__global__ void k_sssp_batch_init(const uint32_t* srcs, int n, float* dist, uint8_t* changed) {
-    const int s = threadIdx.x;
-    if (s < n) {
-        dist[(uint64_t)srcs[s] * 64 + s] = 0.f;
-        changed[srcs[s]] = 1;
-    }
-}
-
 // {src, dst} records -> {src, dst, index} records: the index rides through the build in the weight
 // slot, so every CSR / CSC position knows which input edge it holds
 __global__ void k_expand_ids(const uint2* __restrict__ in, uint64_t E, uint32_t* __restrict__ out) {
