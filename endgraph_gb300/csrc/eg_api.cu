@@ -199,6 +199,7 @@ static int prepare_load(eg_graph* g, uint64_t E, uint32_t V, int edge_bytes, int
     }
     g->built_csr = g->built_csc = false;
     g->eng.pull_ready = false;
+    g->eng.pr_ready = false;
     free_batch_state(g);
     g->batch_voff.clear();
     g->batch_eoff.clear();
@@ -341,6 +342,7 @@ int eg_load_directed_with_ids(eg_graph* g, const void* edges, uint64_t E, uint32
     }
     g->built_csr = g->built_csc = false;
     g->eng.pull_ready = false;
+    g->eng.pr_ready = false;
     free_batch_state(g);
     g->V = V;
     g->E = E;
@@ -579,6 +581,10 @@ int eg_set_option(eg_graph* g, int option, int64_t value) {
         case EG_OPT_SSSP_DELTA:
             if (value < -1 || value > (1ll << 40)) break;
             g->sssp_delta = value;
+            return EG_OK;
+        case EG_OPT_PR_RELABEL:
+            if (value < -1 || value > 1) break;
+            g->pr_relabel = (int)value;
             return EG_OK;
         default:
             set_error("eg_set_option: unknown option %d", option);

@@ -805,6 +805,7 @@ int build_structures(eg_graph* g, int want_csr, int want_csc) {
     const uint64_t nwords = (uint64_t)V / 64 + 1;
     g->built_csr = g->built_csc = false;
     g->eng.pull_ready = false;
+    g->eng.pr_ready = false;
 
     // the bucket tables and a staging tile must fit one CTA's shared memory
     const bool bucketed =

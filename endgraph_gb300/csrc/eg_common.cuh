@@ -114,9 +114,13 @@ struct EngineState {
     DevBuf pull_chunk_item;  // u32 per CSC chunk: first compressed item
     DevBuf pull_split;     // u32 list of vertices whose list spans a chunk boundary
     DevBuf bu_seg;         // u64 segments of the early-exit dense BFS step
+    DevBuf pr_new_id;      // u32 per vertex: position in out-degree-class order (PageRank gathers)
+    DevBuf pr_adj;         // u32 per CSC edge: the source renumbered through pr_new_id
+    DevBuf pr_cnt, pr_off; // class counts per vertex tile and their exclusive scan
     uint64_t pull_nsplit = 0;
     uint64_t pull_nchunks = 0;
     bool pull_ready = false;
+    bool pr_ready = false;  // pr_new_id / pr_adj match the built CSC
     DevBuf host_pinned_dummy;
 };
 
@@ -177,6 +181,7 @@ struct eg_graph {
     int use_cuda_graph = 0; // batched BFS: replay the level loop as one captured CUDA graph
     int pull_blocks_per_sm = 0;  // pull-sweep grid; 0 = occupancy limit
     int batch_width = 64;        // roots per bit-parallel pass (eg_bfs_many)
+    int pr_relabel = -1;         // PageRank gathers through renumbered sources: 1 on, 0 off, -1 automatic
     int64_t sssp_delta = -1;     // SSSP near/far step in millionths; 0 = Bellman-Ford, -1 = automatic
     // many small graphs in one handle (eg_load_graph_batch): per-graph vertex / edge offsets
     std::vector<uint64_t> batch_voff, batch_eoff;

@@ -265,6 +265,7 @@ struct PrPullOp {  // toolkits/pagerank.cpp:64-97: sum curr[src]; next = 1-d+d*s
     float* next;
     float* acc;
     const uint32_t* outdeg;
+    const uint32_t* slot;  // null: next in vertex order; else next[slot[v]] (renumbered order)
     float base, d;
     int divide, single;
     __device__ Acc identity() const { return 0.f; }
@@ -279,7 +280,7 @@ struct PrPullOp {  // toolkits/pagerank.cpp:64-97: sum curr[src]; next = 1-d+d*s
                 uint32_t dg = outdeg[v];
                 if (dg > 0) x /= (float)dg;
             }
-            next[v] = x;
+            next[slot ? slot[v] : v] = x;
         } else {
             atomicAdd(acc + v, a);
         }
@@ -328,25 +329,29 @@ __global__ void k_fill_f32(float* p, uint64_t n, float v) {
 __global__ void k_iota(uint32_t* p, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) p[i] = (uint32_t)i;
 }
-__global__ void k_pr_init(float* curr, const uint32_t* __restrict__ outdeg, uint32_t V) {  // pagerank.cpp:36-45
+// PageRank vectors are kept in vertex order, or (slot non-null) at slot[v]: the renumbering by
+// out-degree class that the gathers go through
+__global__ void k_pr_init(float* curr, const uint32_t* __restrict__ outdeg, uint32_t V,
+                          const uint32_t* __restrict__ slot) {  // pagerank.cpp:36-45
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t dg = outdeg[v];
-        curr[v] = dg > 0 ? 1.0f / (float)dg : 1.0f;
+        curr[slot ? slot[v] : v] = dg > 0 ? 1.0f / (float)dg : 1.0f;
     }
 }
 // vertices without in-edges: next = 1-d (/ outdeg)
 __global__ void k_pr_zero_in(float* buf, const uint32_t* __restrict__ indeg, const uint32_t* __restrict__ outdeg,
-                             uint32_t V, float base, int divide) {
+                             uint32_t V, float base, int divide, const uint32_t* __restrict__ slot) {
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x) {
         if (indeg[v] == 0) {
             uint32_t dg = outdeg[v];
-            buf[v] = (divide && dg > 0) ? base / (float)dg : base;
+            buf[slot ? slot[v] : v] = (divide && dg > 0) ? base / (float)dg : base;
         }
     }
 }
 // destinations whose list crossed a chunk boundary (P == 1)
 __global__ void k_pr_split(const uint32_t* __restrict__ split, const uint32_t* __restrict__ cvert, uint64_t nsplit,
-                           float* next, float* acc, const uint32_t* __restrict__ outdeg, float base, float d, int divide) {
+                           float* next, float* acc, const uint32_t* __restrict__ outdeg, float base, float d, int divide,
+                           const uint32_t* __restrict__ slot) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nsplit; i += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t v = cvert[split[i]];
         float x = base + d * acc[v];
@@ -355,12 +360,13 @@ __global__ void k_pr_split(const uint32_t* __restrict__ split, const uint32_t* _
             uint32_t dg = outdeg[v];
             if (dg > 0) x /= (float)dg;
         }
-        next[v] = x;
+        next[slot ? slot[v] : v] = x;
     }
 }
 // P > 1: every destination with in-edges combines its partial sums
 __global__ void k_pr_finish_all(const uint32_t* __restrict__ indeg, uint32_t V, float* next, float* acc,
-                                const uint32_t* __restrict__ outdeg, float base, float d, int divide) {
+                                const uint32_t* __restrict__ outdeg, float base, float d, int divide,
+                                const uint32_t* __restrict__ slot) {
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x) {
         if (indeg[v] == 0) continue;
         float x = base + d * acc[v];
@@ -369,9 +375,115 @@ __global__ void k_pr_finish_all(const uint32_t* __restrict__ indeg, uint32_t V, 
             uint32_t dg = outdeg[v];
             if (dg > 0) x /= (float)dg;
         }
-        next[v] = x;
+        next[slot ? slot[v] : v] = x;
     }
 }
+
+// ---- renumbering by out-degree class for the PageRank gathers ----------------------------------
+// class = __clz(outdeg): 0 for the largest degrees, 31 for degree 1, 32 for no out-edges (never
+// gathered).  new_id = the vertex's position in class order, tile by tile (tiles of 8,192
+// vertices, classes counted per tile and scanned class-major), in any order inside a tile.
+constexpr uint32_t kRelabelTile = 8192;
+constexpr uint32_t kRelabelClasses = 33;
+constexpr uint32_t kRelabelHot = 1u << 21;  // ranks spread round-robin over the hot region's lines
+
+__global__ void __launch_bounds__(256) k_relabel_hist(const uint32_t* __restrict__ outdeg, uint32_t V, uint32_t ntiles,
+                                                      uint32_t* __restrict__ cnt) {
+    __shared__ uint32_t h[kRelabelClasses];
+    if (threadIdx.x < kRelabelClasses) h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t v0 = (uint64_t)blockIdx.x * kRelabelTile;
+    for (uint32_t i = threadIdx.x; i < kRelabelTile; i += blockDim.x) {
+        const uint64_t v = v0 + i;
+        const uint32_t c = v < V ? (uint32_t)__clz(outdeg[v]) : kRelabelClasses;
+        const uint32_t same = __match_any_sync(0xffffffffu, c);
+        if (c < kRelabelClasses && (threadIdx.x & 31) == (uint32_t)(__ffs(same) - 1)) atomicAdd(&h[c], __popc(same));
+    }
+    __syncthreads();
+    if (threadIdx.x < kRelabelClasses) cnt[(uint64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(256) k_relabel_assign(const uint32_t* __restrict__ outdeg, uint32_t V, uint32_t ntiles,
+                                                        const uint64_t* __restrict__ off, uint32_t lines,
+                                                        uint32_t* __restrict__ new_id) {
+    __shared__ uint32_t cur[kRelabelClasses];
+    if (threadIdx.x < kRelabelClasses) cur[threadIdx.x] = (uint32_t)off[(uint64_t)threadIdx.x * ntiles + blockIdx.x];
+    __syncthreads();
+    const uint64_t v0 = (uint64_t)blockIdx.x * kRelabelTile;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t i = threadIdx.x; i < kRelabelTile; i += blockDim.x) {
+        const uint64_t v = v0 + i;
+        const uint32_t c = v < V ? (uint32_t)__clz(outdeg[v]) : kRelabelClasses;
+        const uint32_t same = __match_any_sync(0xffffffffu, c);
+        const uint32_t leader = (uint32_t)(__ffs(same) - 1);
+        uint32_t base = 0;
+        if (c < kRelabelClasses && lane == leader) base = atomicAdd(&cur[c], __popc(same));
+        base = __shfl_sync(same, base, leader);
+        if (c < kRelabelClasses) {
+            uint32_t r = base + __popc(same & ((1u << lane) - 1u));
+            // the first 32 x lines ranks go round-robin over `lines` 128-byte lines: line j holds
+            // ranks j, j + lines, ... (one vertex per heat stratum), so no line carries all hubs
+            if (r < 32u * lines) r = (r % lines) * 32u + r / lines;
+            new_id[v] = r;
+        }
+    }
+}
+
+// pr_adj[e] = new_id[csc_adj[e]]
+__global__ void __launch_bounds__(256) k_relabel_adj(const uint32_t* __restrict__ adj, uint64_t E,
+                                                     const uint32_t* __restrict__ new_id, uint32_t* __restrict__ out) {
+    const uint64_t nq = E / 4;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < nq; q += stride) {
+        const uint4 s = __ldcs(reinterpret_cast<const uint4*>(adj) + q);
+        __stcs(reinterpret_cast<uint4*>(out) + q, make_uint4(__ldg(new_id + s.x), __ldg(new_id + s.y),
+                                                            __ldg(new_id + s.z), __ldg(new_id + s.w)));
+    }
+    for (uint64_t e = 4 * nq + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += stride)
+        out[e] = __ldg(new_id + adj[e]);
+}
+
+int scan_exclusive_u32(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out);
+
+static bool want_relabel(const eg_graph* g) {
+    return g->pr_relabel > 0 || (g->pr_relabel < 0 && g->V > (1u << 22));
+}
+
+static int setup_relabel(eg_graph* g) {
+    EngineState& s = g->eng;
+    if (s.pr_ready) return EG_OK;
+    const uint32_t V = g->V;
+    const uint64_t E = g->E;
+    const uint32_t ntiles = (uint32_t)(((uint64_t)V + kRelabelTile - 1) / kRelabelTile);
+    const uint64_t ncnt = (uint64_t)kRelabelClasses * ntiles;
+    EG_TRY(s.pr_new_id.reserve(sizeof(uint32_t) * ((size_t)V + 1)));
+    EG_TRY(s.pr_adj.reserve(sizeof(uint32_t) * (E + 32)));
+    EG_TRY(s.pr_cnt.reserve(sizeof(uint32_t) * ncnt));
+    EG_TRY(s.pr_off.reserve(sizeof(uint64_t) * (ncnt + 1)));
+    if (ntiles) {
+        Timed t(&g->prof, g->stream, "pr_relabel");
+        k_relabel_hist<<<ntiles, 256, 0, g->stream>>>(g->outdeg.as<uint32_t>(), V, ntiles, s.pr_cnt.as<uint32_t>());
+        EG_CHECK_LAUNCH("k_relabel_hist");
+    }
+    if (ntiles) EG_TRY(scan_exclusive_u32(g, s.pr_cnt.as<uint32_t>(), ncnt, s.pr_off.as<uint64_t>()));
+    {
+        Timed t(&g->prof, g->stream, "pr_relabel");
+        if (ntiles) {
+            const uint32_t lines = std::min<uint32_t>(V, kRelabelHot) / 32u;
+            k_relabel_assign<<<ntiles, 256, 0, g->stream>>>(g->outdeg.as<uint32_t>(), V, ntiles, s.pr_off.as<uint64_t>(),
+                                                            lines, s.pr_new_id.as<uint32_t>());
+            EG_CHECK_LAUNCH("k_relabel_assign");
+        }
+        if (E) {
+            k_relabel_adj<<<grid_for(E / 4 + 1, 256, 152u * 16u), 256, 0, g->stream>>>(
+                g->csc_adj.as<uint32_t>(), E, s.pr_new_id.as<uint32_t>(), s.pr_adj.as<uint32_t>());
+            EG_CHECK_LAUNCH("k_relabel_adj");
+        }
+    }
+    s.pr_ready = true;
+    return EG_OK;
+}
+
 __global__ void k_bfs_root(uint32_t* level, uint32_t* parent, unsigned long long* visited, unsigned long long* front,
                            uint32_t root, uint32_t* q) {
     if (level) level[root] = 0;
@@ -399,9 +511,14 @@ int run_pagerank(eg_graph* g, int iterations, float damping, float* out, int whe
     const float base = 1.0f - damping;
     const int single = g->partitions == 1;
     const unsigned gv = grid_for(V, 256, 152u * 16u);
+    // with renumbered gathers every vector but the final one is kept in class order
+    const bool relabel = iterations > 0 && g->E > 0 && want_relabel(g);
+    if (relabel) EG_TRY(setup_relabel(g));
+    const uint32_t* order = relabel ? s.pr_new_id.as<uint32_t>() : nullptr;
+    const uint32_t* gather_adj = relabel ? s.pr_adj.as<uint32_t>() : nullptr;
     {
         Timed t(&g->prof, g->stream, "pr_vertex");
-        k_pr_init<<<gv, 256, 0, g->stream>>>(A, g->outdeg.as<uint32_t>(), V);
+        k_pr_init<<<gv, 256, 0, g->stream>>>(A, g->outdeg.as<uint32_t>(), V, order);
         EG_CHECK_LAUNCH("k_pr_init");
         EG_CUDA(cudaMemsetAsync(s.acc.ptr, 0, sizeof(float) * (size_t)V, g->stream));
     }
@@ -409,24 +526,26 @@ int run_pagerank(eg_graph* g, int iterations, float damping, float* out, int whe
         const int last = it == iterations - 1;
         float* curr = (it & 1) ? B : A;
         float* next = (it & 1) ? A : B;
+        const uint32_t* slot = last ? nullptr : order;
         if (it < 2 || last) {
             Timed t(&g->prof, g->stream, "pr_vertex");
-            k_pr_zero_in<<<gv, 256, 0, g->stream>>>(next, g->indeg.as<uint32_t>(), g->outdeg.as<uint32_t>(), V, base, !last);
+            k_pr_zero_in<<<gv, 256, 0, g->stream>>>(next, g->indeg.as<uint32_t>(), g->outdeg.as<uint32_t>(), V, base, !last,
+                                                    slot);
             EG_CHECK_LAUNCH("k_pr_zero_in");
         }
-        PrPullOp op{curr, next, s.acc.as<float>(), g->outdeg.as<uint32_t>(), base, damping, !last, single};
-        EG_TRY(launch_pull(g, op, "pr_pull"));
+        PrPullOp op{curr, next, s.acc.as<float>(), g->outdeg.as<uint32_t>(), slot, base, damping, !last, single};
+        EG_TRY(launch_pull(g, op, "pr_pull", gather_adj));
         Timed t(&g->prof, g->stream, "pr_finish");
         if (single) {
             if (s.pull_nsplit) {
                 k_pr_split<<<grid_for(s.pull_nsplit, 256), 256, 0, g->stream>>>(
                     s.pull_split.as<uint32_t>(), g->cvert.as<uint32_t>(), s.pull_nsplit, next, s.acc.as<float>(),
-                    g->outdeg.as<uint32_t>(), base, damping, !last);
+                    g->outdeg.as<uint32_t>(), base, damping, !last, slot);
                 EG_CHECK_LAUNCH("k_pr_split");
             }
         } else {
             k_pr_finish_all<<<gv, 256, 0, g->stream>>>(g->indeg.as<uint32_t>(), V, next, s.acc.as<float>(),
-                                                       g->outdeg.as<uint32_t>(), base, damping, !last);
+                                                       g->outdeg.as<uint32_t>(), base, damping, !last, slot);
             EG_CHECK_LAUNCH("k_pr_finish_all");
         }
     }

@@ -56,8 +56,9 @@ static int setup_pull(eg_graph* g) {
     return EG_OK;
 }
 
+// adj: the CSC source ids to gather through (default: the built CSC's)
 template <class Op>
-static int launch_pull(eg_graph* g, const Op& op, const char* name) {
+static int launch_pull(eg_graph* g, const Op& op, const char* name, const uint32_t* adj = nullptr) {
     EngineState& s = g->eng;
     const uint64_t nitems = g->ncompressed - 1;
     if (s.pull_nchunks == 0) return EG_OK;
@@ -70,7 +71,7 @@ static int launch_pull(eg_graph* g, const Op& op, const char* name) {
     if (g->pull_blocks_per_sm > 0) per_sm = std::min(per_sm, g->pull_blocks_per_sm);
     unsigned grid = (unsigned)std::min<uint64_t>(s.pull_nchunks, (uint64_t)g->num_sms * (uint64_t)std::max(per_sm, 1));
     Timed t(&g->prof, g->stream, name);
-    k_pull<Op><<<grid, kPullThreads, smem, g->stream>>>(op, g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(),
+    k_pull<Op><<<grid, kPullThreads, smem, g->stream>>>(op, adj ? adj : g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(),
                                                         g->cvert.as<uint32_t>(), s.pull_chunk_item.as<uint32_t>(), g->E,
                                                         nitems, s.pull_nchunks, g->V, cap);
     EG_CHECK_LAUNCH(name);

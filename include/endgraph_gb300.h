@@ -183,9 +183,14 @@ enum {
     EG_OPT_CUDA_GRAPH = 3,
     EG_OPT_PULL_BLOCKS_PER_SM = 4, /* pull-sweep CTAs per SM, 0 = occupancy limit */
     EG_OPT_BATCH_WIDTH = 5,        /* roots per bit-parallel pass of eg_bfs_many, 1..64 */
-    EG_OPT_SSSP_DELTA = 6          /* eg_sssp near/far step in millionths of a weight unit; 0 = plain
+    EG_OPT_SSSP_DELTA = 6,         /* eg_sssp near/far step in millionths of a weight unit; 0 = plain
                                       Bellman-Ford sweeps (the reference's order), -1 = automatic
                                       (0.7 x mean weight / mean out-degree; the default) */
+    EG_OPT_PR_RELABEL = 7          /* eg_pagerank gathers through a copy of the CSC source ids
+                                      renumbered by out-degree class, high degrees first, so that
+                                      the values most gathered share cache lines; the same values
+                                      are summed per destination.  1 on, 0 off, -1 automatic (on
+                                      for V > 2^22; the default) */
 };
 int eg_set_option(eg_graph* g, int option, int64_t value);
 

@@ -80,6 +80,36 @@ def test_pagerank(eg_lib, V, E, seed, P):
     assert err <= 1e-6, err
 
 
+@pytest.mark.parametrize("P", [1, 3])
+def test_pagerank_renumbered_gathers(eg_lib, P):
+    """Gathering through sources renumbered by out-degree class sums the same values: the ranks
+    match the vertex-order run for 0, 1, 2 and 20 iterations (up to the order of the float
+    additions, which the shared-memory partial sums leave open in both), and a rebuild renumbers
+    again."""
+    import endgraph_gb300 as eg
+    V, E = 50_000, 600_000
+    src, dst, _ = rmat_graph(V, E, 77)
+    o_out, _ = oracle.degrees(src, dst, V)
+    csc = oracle.build_csc(src, dst, None, V, np.array([0, V], np.uint32))
+    with _graph(eg_lib, P=P) as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        for iters in (0, 1, 2, 20):
+            g.set_option(eg.EG_OPT_PR_RELABEL, 0)
+            plain = g.pagerank(iters, 0.85)
+            g.set_option(eg.EG_OPT_PR_RELABEL, 1)
+            ren = g.pagerank(iters, 0.85)
+            assert rel_l1(ren, plain) <= 1e-6, iters
+        ref = oracle.pagerank(csc["off"][0], csc["adj"], o_out, V, 20, 0.85)
+        assert rel_l1(ren, ref) <= 1e-6
+        # a second graph on the same handle: the renumbering follows the new degrees
+        src2, dst2, _ = rmat_graph(V, E // 2, 78)
+        g.load_directed(eg.pack_edges(src2, dst2), V)
+        o2, _ = oracle.degrees(src2, dst2, V)
+        csc2 = oracle.build_csc(src2, dst2, None, V, np.array([0, V], np.uint32))
+        ref2 = oracle.pagerank(csc2["off"][0], csc2["adj"], o2, V, 20, 0.85)
+        assert rel_l1(g.pagerank(20, 0.85), ref2) <= 1e-6
+
+
 @pytest.mark.parametrize("V,E,seed", CASES)
 @pytest.mark.parametrize("P", [1, 2])
 def test_bfs(eg_lib, V, E, seed, P):
