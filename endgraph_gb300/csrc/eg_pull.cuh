@@ -64,7 +64,7 @@ static int launch_pull(eg_graph* g, const Op& op, const char* name, const uint32
     if (s.pull_nchunks == 0) return EG_OK;
     // a chunk holds at most one item per edge plus the zero-length sentinels of empty partitions
     const int cap = (int)kPullChunk + g->partitions + 2;
-    const size_t smem = align16(sizeof(uint32_t) * (cap + 1)) + sizeof(typename Op::Acc) * cap + (Op::kFilter ? cap : 0);
+    const size_t smem = pull_acc_offset(cap) + sizeof(typename Op::Acc) * cap + (Op::kFilter ? cap : 0);
     EG_CUDA(cudaFuncSetAttribute(k_pull<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<Op>, kPullThreads, smem));

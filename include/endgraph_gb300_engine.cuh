@@ -514,7 +514,7 @@ class Engine {
         detail::PullAdapter<Op> pa{op, sd.pull_w, static_cast<Acc*>(partial_), out, P_ == 1 ? 1 : 0};
         using K = detail::PullAdapter<Op>;
         const int cap = (int)kPullChunk + P_ + 2;
-        const size_t smem = align16(sizeof(uint32_t) * (cap + 1)) + sizeof(Acc) * cap + cap;
+        const size_t smem = pull_acc_offset(cap) + sizeof(Acc) * cap + cap;
         check(cudaFuncSetAttribute(k_pull<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem");
         int per_sm = 0;
         check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<K>, kPullThreads, smem), "occupancy");

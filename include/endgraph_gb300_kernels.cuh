@@ -193,6 +193,11 @@ static __global__ void k_pull_chunks(const uint64_t* __restrict__ cidx, const ui
     if (blockIdx.x == 0 && threadIdx.x == 0) chunk_item[nchunks] = (uint32_t)nitems;
 }
 
+// k_pull's shared memory: cap + 1 item boundaries (u16, relative to the chunk start, <= kPullChunk),
+// then cap accumulators, then cap filter bytes when Op::kFilter.  The smaller the footprint, the
+// larger the L1 share of the SM's unified L1/shared memory that caches the gathers.
+__host__ __device__ constexpr size_t pull_acc_offset(int cap) { return align16(sizeof(uint16_t) * (cap + 1)); }
+
 // Generic segmented pull over compressed CSC entries.  Op provides:
 //   Acc identity(); Acc gather(uint32_t src, uint64_t epos); Acc combine(Acc, Acc);
 //   void smem_add(Acc* slot, Acc v); void finish(uint32_t v, Acc a, bool whole)
@@ -206,8 +211,8 @@ __global__ void __launch_bounds__(kPullThreads, 3) k_pull(Op op, const uint32_t*
     if (op.stopped()) return;  // a captured loop whose traversal already finished
     extern __shared__ __align__(16) unsigned char s_raw[];
     // item boundaries relative to the chunk start, clamped to [0, chunk]: 4 bytes per item
-    uint32_t* s_idx = reinterpret_cast<uint32_t*>(s_raw);
-    Acc* s_acc = reinterpret_cast<Acc*>(s_raw + align16(sizeof(uint32_t) * (cap + 1)));
+    uint16_t* s_idx = reinterpret_cast<uint16_t*>(s_raw);
+    Acc* s_acc = reinterpret_cast<Acc*>(s_raw + pull_acc_offset(cap));
     uint8_t* s_on = reinterpret_cast<uint8_t*>(s_acc + cap);  // per-item filter (Op::kFilter)
     for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const uint64_t e0 = c * kPullChunk;
@@ -220,7 +225,7 @@ __global__ void __launch_bounds__(kPullThreads, 3) k_pull(Op op, const uint32_t*
         const bool last_open = cidx[iend] > e1;    // last item continues into a later chunk
         for (int k = threadIdx.x; k <= nit; k += blockDim.x) {
             const uint64_t x = cidx[i0 + k];
-            s_idx[k] = x <= e0 ? 0u : (x >= e1 ? (uint32_t)(e1 - e0) : (uint32_t)(x - e0));
+            s_idx[k] = (uint16_t)(x <= e0 ? 0u : (x >= e1 ? (uint32_t)(e1 - e0) : (uint32_t)(x - e0)));
             if (k < nit) {
                 s_acc[k] = op.identity();
                 if (Op::kFilter) {
