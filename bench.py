@@ -41,6 +41,9 @@ def parse_args():
     p.add_argument("--scale", type=int, default=25)
     p.add_argument("--edge-factor", type=int, default=16)
     p.add_argument("--pr-iters", type=int, default=20)
+    p.add_argument("--pr-relabel", type=int, default=-1, choices=[-1, 0, 1],
+                   help="PageRank gathers through sources renumbered by out-degree class: "
+                        "1 on, 0 off (vertex order), -1 automatic (on for V > 2^22)")
     p.add_argument("--roots", type=int, default=16)
     p.add_argument("--seed", type=int, default=20240601)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -451,6 +454,7 @@ def run_ours(args, world, rank, local):
     roots = roots_all[:args.roots]
 
     g = eg.Graph(eta=1, partitions=1, max_iterations=args.pr_iters, device=local)
+    g.set_option(eg.EG_OPT_PR_RELABEL, args.pr_relabel)
     g.load_edges(edges, V)
     stream = torch.cuda.ExternalStream(g.stream, device=dev)
     pr_out = torch.empty(V, dtype=torch.float32, device=dev)

@@ -202,7 +202,7 @@ __host__ __device__ constexpr size_t pull_acc_offset(int cap) { return align16(s
 //   Acc identity(); Acc gather(uint32_t src, uint64_t epos); Acc combine(Acc, Acc);
 //   void smem_add(Acc* slot, Acc v); void finish(uint32_t v, Acc a, bool whole)
 template <class Op>
-__global__ void __launch_bounds__(kPullThreads, 3) k_pull(Op op, const uint32_t* __restrict__ adj,
+__global__ void __launch_bounds__(kPullThreads, 5) k_pull(Op op, const uint32_t* __restrict__ adj,
                                                         const uint64_t* __restrict__ cidx,
                                                         const uint32_t* __restrict__ cvert,
                                                         const uint32_t* __restrict__ chunk_item, uint64_t E,
