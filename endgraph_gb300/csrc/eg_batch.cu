@@ -193,9 +193,12 @@ struct MsBfsPushOp {
 
 // level bytes of the queued vertices' new bits (row v of [V][64]: 16 threads, one 4-byte word
 // each) and the OR of their words, i.e. the roots whose traversal is still running
+// With new_id, the words are also copied to renumbered positions (next_r[new_id[v]]) for the pull
+// gathers that go through the renumbered CSC sources.
 __global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n_dev,
                                const unsigned long long* __restrict__ next, uint8_t* levels, uint32_t lvl,
-                               unsigned long long* alive_out) {
+                               unsigned long long* alive_out, const uint32_t* __restrict__ new_id,
+                               unsigned long long* __restrict__ next_r) {
     const uint32_t n = __ldcg(n_dev);
     const uint32_t sub = threadIdx.x & 15;
     const uint32_t fill = (lvl & 0xFFu) * 0x01010101u;
@@ -204,6 +207,7 @@ __global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n
          i += ((uint64_t)gridDim.x * blockDim.x) >> 4) {
         const uint32_t v = q[i];
         const unsigned long long nb = next[v];
+        if (new_id && sub == 0) next_r[new_id[v]] = nb;
         orr |= nb;
         const uint32_t nib = (uint32_t)(nb >> (4 * sub)) & 0xFu;
         if (levels && nib) {
@@ -217,6 +221,15 @@ __global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) orr |= __shfl_xor_sync(0xffffffffu, orr, o);
     if ((threadIdx.x & 31) == 0 && orr) atomicOr(alive_out, orr);
+}
+
+// the renumbered copy of the first frontier (the roots), which no level has listed
+__global__ void k_front_renumber(const uint32_t* __restrict__ q, const uint32_t* n_dev,
+                                 const unsigned long long* __restrict__ word, const uint32_t* __restrict__ new_id,
+                                 unsigned long long* __restrict__ word_r) {
+    const uint32_t n = __ldcg(n_dev);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        word_r[new_id[q[i]]] = word[q[i]];
 }
 
 // sum over vertices of popcount(visited word) * out-degree: the edges 64 single-root runs scan
@@ -624,6 +637,7 @@ int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E) {
 struct BatchState {
     DevBuf a64, b64, c64, lev, rows0, rows1, heavy, tmp_out, seeds, wn_csc, wn_csr, s_out, gA, row_of, ck, seg;
     DevBuf ch0, ch1, flag, level_cnt, entries, n_entries, bm0, bm1, alive, ms_seg;
+    DevBuf wr0, wr1;  // frontier words in renumbered order (pull gathers through renumbered sources)
     RowTasks csc_tasks, csr_tasks;
     bool csc_ready = false, csr_ready = false;
     // captured MS-BFS level loop and the shapes it was captured for
@@ -734,6 +748,18 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
     const uint32_t* deg = g->outdeg.as<uint32_t>();
     const unsigned init_grid = std::max(1u, std::min<unsigned>((n_entries + 255) / 256, 4096u));
     const unsigned grid = (unsigned)g->num_sms * 8u;
+    const bool one_graph = g->batch_voff.empty();
+    // pull gathers through the CSC sources renumbered by out-degree class (hot frontier words share
+    // cache lines), with a renumbered copy of each frontier; on one graph with the host-driven loop
+    const bool renum = one_graph && !g->use_cuda_graph && g->E > 0 && want_relabel(g);
+    if (renum) {
+        EG_TRY(setup_relabel(g));
+        EG_TRY(b.wr0.reserve(8 * V + 8));
+        EG_TRY(b.wr1.reserve(8 * V + 8));
+    }
+    unsigned long long* word_r[2] = {b.wr0.as<unsigned long long>(), b.wr1.as<unsigned long long>()};
+    const uint32_t* new_id = s.pr_new_id.as<uint32_t>();
+    const uint32_t* gather_adj = renum ? s.pr_adj.as<uint32_t>() : g->csc_adj.as<uint32_t>();
 
     auto enqueue_init = [&]() -> int {
         EG_CUDA(cudaMemsetAsync(visit, 0, 8 * V, g->stream));
@@ -747,6 +773,11 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         k_msbfs_init_entries<<<init_grid, 256, 0, g->stream>>>(b.entries.as<uint2>(), b.n_entries.as<uint32_t>(), visit,
                                                                word[0], bm[0], lev, queue[0], d_nq, d_act, deg);
         EG_CHECK_LAUNCH("k_msbfs_init_entries");
+        if (renum) {
+            EG_CUDA(cudaMemsetAsync(word_r[0], 0, 8 * V, g->stream));
+            k_front_renumber<<<init_grid, 256, 0, g->stream>>>(queue[0], d_nq, word[0], new_id, word_r[0]);
+            EG_CHECK_LAUNCH("k_front_renumber");
+        }
         return EG_OK;
     };
     // one level L: frontier word[L&1] / bm[L&1] / queue[L&1] -> the same of parity (L+1)&1.  The
@@ -757,12 +788,17 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
     // dense levels find most destinations nearly covered and use the early-exit pair -- on one
     // graph.  In a batch of graphs the running-root mask is shared by all graphs, so a vertex
     // waits for bits its own graph can never deliver, and every level keeps the chunked sweep.
-    const bool one_graph = g->batch_voff.empty();
     auto enqueue_level = [&](uint32_t L, uint64_t n_host, bool dense, bool screen, uint32_t* count, const int* stop_flag,
                              uint32_t* nout_host, unsigned long long* act_host, bool early_exit) -> int {
         const int c = L & 1, x = c ^ 1;
         EG_CUDA(cudaMemsetAsync(word[x], 0, 8 * V, g->stream));
         EG_CUDA(cudaMemsetAsync(bm[x], 0, bm_bytes, g->stream));
+        // renumbered gathers skip the frontier-bitmap screen (dense levels rarely screen)
+        const unsigned long long* gather_word = renum ? word_r[c] : word[c];
+        if (renum) {
+            screen = false;
+            EG_CUDA(cudaMemsetAsync(word_r[x], 0, 8 * V, g->stream));
+        }
         unsigned long long* alive_next = stop_flag ? nullptr : alive + x;
         if (alive_next) EG_CUDA(cudaMemsetAsync(alive_next, 0, 8, g->stream));
         if (dense) {
@@ -771,8 +807,8 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
             if (early_exit) {
                 uint32_t* d_nseg = reinterpret_cast<uint32_t*>(cnt + kGraphLevels + 2);
                 EG_CUDA(cudaMemsetAsync(d_nseg, 0, 4, g->stream));
-                MsBuArgs ma{g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(),
-                            g->ncompressed - 1, (uint32_t)V, word[c], visit, word[x], bm[x],
+                MsBuArgs ma{gather_adj, g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(),
+                            g->ncompressed - 1, (uint32_t)V, gather_word, visit, word[x], bm[x],
                             stop_flag ? alive + 2 : alive + c, b.ms_seg.as<unsigned long long>(), d_nseg, stop_flag};
                 Timed t(&g->prof, g->stream, "msbfs_pull");
                 k_ms_head<<<grid_for(ma.nitems, 256, grid), 256, 0, g->stream>>>(ma);
@@ -780,9 +816,9 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
                 k_ms_tail<<<grid, 256, 0, g->stream>>>(ma);
                 EG_CHECK_LAUNCH("k_ms_tail");
             } else {
-                MsBfsPullOp op{word[c], bm[c], screen ? 1 : 0, visit, word[x], bm[x],
+                MsBfsPullOp op{gather_word, bm[c], screen ? 1 : 0, visit, word[x], bm[x],
                                stop_flag ? alive + 2 : alive + c, stop_flag};
-                EG_TRY(launch_pull_direct(g, op, "msbfs_pull"));
+                EG_TRY(launch_pull_direct(g, op, "msbfs_pull", gather_adj));
             }
             Timed t(&g->prof, g->stream, "msbfs_vertex");
             k_bm_compact<<<grid_for(nwords, 256, grid), 256, 0, g->stream>>>(bm[x], nwords, queue[x], count,
@@ -792,9 +828,10 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
             MsBfsPushOp op{word[c], visit, word[x], bm[x]};
             EG_TRY(push_level(g, op, queue[c], n_host, queue[x], nout_host, nullptr, act_host, deg, "msbfs_push"));
         }
-        if (lev || alive_next) {
+        if (lev || alive_next || renum) {
             Timed t(&g->prof, g->stream, "msbfs_vertex");
-            k_queue_levels<<<grid, 256, 0, g->stream>>>(queue[x], count, word[x], lev, L + 1, alive_next);
+            k_queue_levels<<<grid, 256, 0, g->stream>>>(queue[x], count, word[x], lev, L + 1, alive_next,
+                                                        renum ? new_id : nullptr, word_r[x]);
             EG_CHECK_LAUNCH("k_queue_levels");
         }
         return EG_OK;

@@ -208,6 +208,10 @@ int selftest_bounded_wait(eg_graph* g, uint32_t spin_cap);
 int validate_edges(eg_graph* g, uint64_t E);
 int symmetrize_edges(eg_graph* g, uint64_t E);
 int run_pagerank(eg_graph* g, int iterations, float damping, float* out, int where);
+// renumbering of the CSC sources by out-degree class (eng.pr_new_id / eng.pr_adj), built once per
+// structure build and shared by the PageRank and bit-parallel BFS pull gathers
+bool want_relabel(const eg_graph* g);
+int setup_relabel(eg_graph* g);
 int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int where, uint64_t* reached);
 int run_sssp(eg_graph* g, uint32_t root, float* dist, int where);
 int run_cc(eg_graph* g, uint32_t* label, int where);

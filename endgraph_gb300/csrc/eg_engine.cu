@@ -445,11 +445,11 @@ __global__ void __launch_bounds__(256) k_relabel_adj(const uint32_t* __restrict_
 
 int scan_exclusive_u32(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out);
 
-static bool want_relabel(const eg_graph* g) {
+bool want_relabel(const eg_graph* g) {
     return g->pr_relabel > 0 || (g->pr_relabel < 0 && g->V > (1u << 22));
 }
 
-static int setup_relabel(eg_graph* g) {
+int setup_relabel(eg_graph* g) {
     EngineState& s = g->eng;
     if (s.pr_ready) return EG_OK;
     const uint32_t V = g->V;

@@ -12,8 +12,9 @@
 
 namespace eg {
 
+// adj: the CSC source ids to gather through (default: the built CSC's)
 template <class Op>
-static int launch_pull_direct(eg_graph* g, const Op& op, const char* name) {
+static int launch_pull_direct(eg_graph* g, const Op& op, const char* name, const uint32_t* adj = nullptr) {
     EngineState& s = g->eng;
     if (s.pull_nchunks == 0) return EG_OK;
     const uint64_t nitems = g->ncompressed - 1;
@@ -22,8 +23,8 @@ static int launch_pull_direct(eg_graph* g, const Op& op, const char* name) {
     EG_CUDA(cudaFuncSetAttribute(k_pull_direct<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     Timed t(&g->prof, g->stream, name);
     k_pull_direct<Op><<<(unsigned)s.pull_nchunks, kPullThreads, smem, g->stream>>>(
-        op, g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(), s.pull_chunk_item.as<uint32_t>(),
-        g->E, nitems, g->V);
+        op, adj ? adj : g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(),
+        s.pull_chunk_item.as<uint32_t>(), g->E, nitems, g->V);
     EG_CHECK_LAUNCH(name);
     return EG_OK;
 }

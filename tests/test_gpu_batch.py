@@ -30,6 +30,34 @@ def test_msbfs_matches_single_source(eg_lib):
         assert edges == total
 
 
+@pytest.mark.parametrize("direction_div", [20, 1, 1 << 30])  # Gemini's switch, all push, all pull
+def test_msbfs_renumbered_gathers(eg_lib, direction_div):
+    """Pull levels that gather through the renumbered CSC sources (and the renumbered copy of each
+    frontier) give the same levels and edge count as vertex-order gathers, level by level."""
+    import endgraph_gb300 as eg
+    V, E = 1 << 14, 1 << 18
+    src, dst, _ = rmat_graph(V, E, 93)
+    csr = oracle.build_csr(src, dst, None, V, np.array([0, V], np.uint32))
+    rng = np.random.default_rng(5)
+    roots = src[rng.integers(0, E, 64)].astype(np.uint32)
+    with eg.Graph() as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        g.set_option(eg.EG_OPT_DENSE_DIVISOR, direction_div)
+        g.set_option(eg.EG_OPT_PR_RELABEL, 0)
+        plain, e_plain = g.msbfs(roots)
+        g.set_option(eg.EG_OPT_PR_RELABEL, 1)
+        ren, e_ren = g.msbfs(roots)
+        assert np.array_equal(plain, ren) and e_plain == e_ren
+        for s in (0, 17, 63):
+            ref = oracle.bfs_levels(csr["off"][0], csr["adj"], V, int(roots[s]))
+            assert np.array_equal(ren[s], np.where(ref == oracle.UNREACHED, 255, ref).astype(np.uint8))
+        run = g.last_run()
+        if direction_div == 1:
+            assert run["pull"] == 0
+        if direction_div == 1 << 30:
+            assert run["push"] == 0
+
+
 @pytest.mark.parametrize("cuda_graph", [0, 1])
 def test_msbfs_cuda_graph_mode(eg_lib, cuda_graph):
     """The captured 32-level loop gives the same levels as the host-driven loop."""
