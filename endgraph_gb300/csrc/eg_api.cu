@@ -69,6 +69,13 @@ void free_handle(eg_graph* g) {
     g->prof.clear();
     free_batch_state(g);
     if (g->pinned) cudaFreeHost(g->pinned);
+    if (g->copy_stream) {
+        cudaStreamSynchronize(g->copy_stream);
+        cudaStreamDestroy(g->copy_stream);
+    }
+    for (cudaEvent_t e : g->part_ready)
+        if (e) cudaEventDestroy(e);
+    if (g->copy_gate) cudaEventDestroy(g->copy_gate);
     cudaStream_t s = g->stream;
     bool own = g->own_stream;
     delete g;  // DevBuf destructors free device memory
@@ -179,6 +186,44 @@ int load_edges_impl(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int 
     }
     if (validate) EG_TRY(validate_edges(g, E));
     if (symmetric) EG_TRY(symmetrize_edges(g, E));
+    return EG_OK;
+}
+
+// Host records uploaded in up to 8 parts on the handle's copy stream while the build consumes
+// them: passes A and B of part k (and the id validation, in pass A) run on the handle's stream as
+// soon as part k has landed, so only the last part's passes and pass C follow the upload.  The
+// caller's buffer is read until this returns.
+int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes) {
+    EG_TRY(prepare_load(g, E, V, edge_bytes, 0));
+    if (!g->copy_stream) EG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    if (!g->copy_gate) EG_CUDA(cudaEventCreateWithFlags(&g->copy_gate, cudaEventDisableTiming));
+    for (cudaEvent_t& e : g->part_ready)
+        if (!e) EG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    UploadParts up{};
+    up.K = (int)std::max<uint64_t>(1, std::min<uint64_t>(8, E / (kPipelinedLoadMin / 2)));
+    const uint64_t per = ((E + up.K - 1) / up.K + 63) & ~63ull;  // parts start on 64-record boundaries
+    int K = 0;
+    for (uint64_t a = 0; a < E && K < 8; a += per) up.e0[K++] = a;
+    up.K = K;
+    up.e0[K] = E;
+    // the records buffer may still be read by earlier work on the handle's stream
+    EG_CUDA(cudaEventRecord(g->copy_gate, g->stream));
+    EG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->copy_gate, 0));
+    const uint8_t* src = static_cast<const uint8_t*>(edges);
+    for (int k = 0; k < K; ++k) {
+        const size_t off = (size_t)up.e0[k] * edge_bytes, n = (size_t)(up.e0[k + 1] - up.e0[k]) * edge_bytes;
+        EG_CUDA(cudaMemcpyAsync(g->edges.as<uint8_t>() + off, src + off, n, cudaMemcpyHostToDevice, g->copy_stream));
+        EG_CUDA(cudaEventRecord(g->part_ready[k], g->copy_stream));
+        up.ready[k] = g->part_ready[k];
+    }
+    free_batch_state(g);
+    const int st = build_structures(g, 1, 1, &up);
+    const cudaError_t e = cudaStreamSynchronize(g->copy_stream);  // never return with the buffer in use
+    if (st != EG_OK) {
+        g->V = 0;  // no usable edge list
+        return st;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
     return EG_OK;
 }
 
@@ -385,6 +430,10 @@ int eg_sssp_batch(eg_graph* g, const uint32_t* sources, int nsources, float* dis
 }
 
 int eg_load_directed(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes, int where) {
+    if (where == EG_HOST && E >= eg::kPipelinedLoadMin && edges) {
+        EG_TRY(check_graph(g, "eg_load_directed"));
+        return eg::load_build_pipelined(g, edges, E, V, edge_bytes);
+    }
     EG_TRY(eg_load_edges(g, edges, E, V, edge_bytes, 0, where));
     return eg_build(g, 1, 1);
 }

@@ -298,29 +298,37 @@ constexpr int kBuildThreads = 1024;
 constexpr uint32_t kMaxBucketVerts = 32768;  // 128 KiB of shared-memory counters in pass C
 constexpr int kBuildUnroll = 4;
 
+// Records holding an id >= V are counted nowhere (pass B skips the same records) and raise *bad:
+// a load that uploads and builds in one pipeline validates here instead of in a separate pass.
 template <int REC>
 __global__ void __launch_bounds__(kBucketThreads) k_bucket_hist(const uint8_t* __restrict__ edges, uint64_t E,
                                                                  uint64_t chunk, int shift, uint32_t nb, uint32_t nblk,
-                                                                 uint32_t* __restrict__ cnt) {
+                                                                 uint32_t* __restrict__ cnt, uint32_t V, int* bad) {
     extern __shared__ uint32_t s_h[];  // [2][nb]
     for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_h[i] = 0;
     __syncthreads();
     const uint64_t e0 = blockIdx.x * chunk;
     const uint64_t e1 = e0 + chunk < E ? e0 + chunk : E;
+    bool out_of_range = false;
+    auto count = [&](uint32_t s, uint32_t d) {
+        if (s < V && d < V) {
+            atomicAdd(&s_h[s >> shift], 1u);
+            atomicAdd(&s_h[nb + (d >> shift)], 1u);
+        } else {
+            out_of_range = true;
+        }
+    };
     if (REC == 8) {
         // two records per 16-byte load (chunk is even, the buffer is 16-byte aligned)
         const uint4* p = reinterpret_cast<const uint4*>(edges);
         for (uint64_t e = e0 + 2 * threadIdx.x; e < e1; e += 2 * blockDim.x) {
             if (e + 1 < e1) {
                 uint4 x = __ldcs(p + e / 2);
-                atomicAdd(&s_h[x.x >> shift], 1u);
-                atomicAdd(&s_h[nb + (x.y >> shift)], 1u);
-                atomicAdd(&s_h[x.z >> shift], 1u);
-                atomicAdd(&s_h[nb + (x.w >> shift)], 1u);
+                count(x.x, x.y);
+                count(x.z, x.w);
             } else {
                 uint2 x = reinterpret_cast<const uint2*>(edges)[e];
-                atomicAdd(&s_h[x.x >> shift], 1u);
-                atomicAdd(&s_h[nb + (x.y >> shift)], 1u);
+                count(x.x, x.y);
             }
         }
     } else {
@@ -328,25 +336,13 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_hist(const uint8_t* _
             uint32_t s, d;
             float w;
             load_edge<REC>(edges, e, s, d, w);
-            atomicAdd(&s_h[s >> shift], 1u);
-            atomicAdd(&s_h[nb + (d >> shift)], 1u);
+            count(s, d);
         }
     }
+    if (out_of_range) atomicExch(bad, 1);
     __syncthreads();
     // bucket-major layout: [half][bucket][block]
     for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) cnt[(uint64_t)i * nblk + blockIdx.x] = s_h[i];
-}
-
-template <int REC>
-__device__ __forceinline__ void store_rec(uint8_t* out, uint64_t pos, uint32_t s, uint32_t d, float w) {
-    if (REC == 8) {
-        reinterpret_cast<uint2*>(out)[pos] = make_uint2(s, d);
-    } else {
-        uint32_t* r = reinterpret_cast<uint32_t*>(out + pos * 12u);
-        r[0] = s;
-        r[1] = d;
-        r[2] = __float_as_uint(w);
-    }
 }
 
 // in-place exclusive scan of s[0..n) by the whole block; returns the total
@@ -393,11 +389,13 @@ constexpr int kScatterThreads = 1024;
 __host__ __device__ constexpr int scatter_per(int rec) { return rec == 8 ? 16 : 8; }
 __host__ __device__ constexpr int scatter_tile(int rec) { return kScatterThreads * scatter_per(rec); }
 
-template <int REC>
+// kCheck: skip records with an id >= V as pass A did (an upload validated in pass A); edge lists
+// validated at load leave it off
+template <int REC, bool kCheck>
 __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_t* __restrict__ edges, uint64_t E,
                                                                     uint64_t chunk, int shift, uint32_t nb, uint32_t nblk,
                                                                     const uint64_t* __restrict__ excl,
-                                                                    uint8_t* __restrict__ out) {
+                                                                    uint8_t* __restrict__ out, uint32_t V) {
     constexpr int W = REC / 4;  // words per record
     extern __shared__ __align__(16) unsigned char s_raw[];
     unsigned long long* s_base = reinterpret_cast<unsigned long long*>(s_raw);  // [2][nb]
@@ -421,6 +419,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_
                 const uint32_t* r = reinterpret_cast<const uint32_t*>(edges + e * REC);
 #pragma unroll
                 for (int w = 0; w < W; ++w) rec[j][w] = __ldcs(r + w);
+                if (kCheck) valid[j] = rec[j][0] < V && rec[j][1] < V;  // pass A skipped it too
             }
         }
 #pragma unroll
@@ -523,15 +522,28 @@ __device__ __forceinline__ void st_keep_u32(uint32_t* p, uint32_t v, unsigned lo
     asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(policy) : "memory");
 }
 
+// The bucketed records of a build come in K parts (an upload in pieces scatters each piece as it
+// lands): part k holds 2 x E_k records from record 2 * e0_k on, bucket-sorted per half, with
+// excl[k] its exclusive scan over (half, bucket, block) of nblk[k] blocks (entry 2 * nb * nblk[k]
+// the part's total).  Bucket b of half h is the union over k of
+// [2 e0_k + excl_k[(h nb + b) nblk_k], 2 e0_k + excl_k[(h nb + b + 1) nblk_k]).
+constexpr int kMaxParts = 8;
+struct BuildParts {
+    int K;
+    uint64_t base2[kMaxParts];          // 2 * e0_k
+    const uint64_t* excl[kMaxParts];
+    uint32_t nblk[kMaxParts];
+};
+
 // C: one bucket per CTA iteration (persistent CTAs take buckets from a ticket)
 template <int REC>
-__global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* __restrict__ rec, const uint64_t* __restrict__ excl,
-                                                                 uint64_t half_base, uint64_t E, uint32_t nb, uint32_t nblk,
-                                                                 uint32_t LB, uint32_t V, int key_is_src,
+__global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* __restrict__ rec, BuildParts parts,
+                                                                 int half, uint32_t nb, uint32_t LB, uint32_t V,
                                                                  uint32_t* __restrict__ deg, uint64_t* __restrict__ off,
                                                                  uint32_t* __restrict__ adj, float* __restrict__ wout,
-                                                                 uint32_t* ticket, int vec_ok) {
-    const bool vec = vec_ok != 0;
+                                                                 uint32_t* ticket) {
+    const bool vec = REC == 8;  // the bucketed buffer is 16-byte aligned
+    const bool key_is_src = half == 0;
     // the 4-byte placement stores land at random positions of the bucket's window: ask L2 to keep
     // those lines so that a partly written sector is usually completed before it is evicted
     unsigned long long keep;
@@ -539,20 +551,36 @@ __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* _
     extern __shared__ uint32_t s_cnt[];  // LB counters
     __shared__ uint32_t s_warp[32];
     __shared__ uint32_t s_b;
+    __shared__ uint64_t s_lo[kMaxParts], s_hi[kMaxParts];
+    __shared__ uint64_t s_r0, s_r1;
     while (true) {
         if (threadIdx.x == 0) s_b = atomicAdd(ticket, 1u);
         __syncthreads();
         const uint32_t b = s_b;
         if (b >= nb) break;
+        if (threadIdx.x == 0) {
+            uint64_t r0 = 0, len = 0;
+            for (int k = 0; k < parts.K; ++k) {
+                const uint64_t* ex = parts.excl[k];
+                const uint64_t nbk = parts.nblk[k];
+                const uint64_t lo = ex[((uint64_t)half * nb + b) * nbk], hi = ex[((uint64_t)half * nb + b + 1) * nbk];
+                r0 += lo - ex[(uint64_t)half * nb * nbk];  // this part's records of earlier buckets
+                len += hi - lo;
+                s_lo[k] = parts.base2[k] + lo;
+                s_hi[k] = parts.base2[k] + hi;
+            }
+            s_r0 = r0;
+            s_r1 = r0 + len;
+        }
         const uint32_t v0 = b * LB;
         const uint32_t nv = V - v0 < LB ? V - v0 : LB;
-        const uint64_t r0 = excl[(uint64_t)b * nblk] - half_base;
-        const uint64_t r1 = b + 1 < nb ? excl[(uint64_t)(b + 1) * nblk] - half_base : E;
         for (uint32_t i = threadIdx.x; i < nv; i += blockDim.x) s_cnt[i] = 0;
         __syncthreads();
-        for_records<REC>(rec, r0, r1, vec, [&](uint32_t s, uint32_t d, uint32_t) {
-            atomicAdd(&s_cnt[(key_is_src ? s : d) - v0], 1u);
-        });
+        const uint64_t r0 = s_r0, r1 = s_r1;
+        for (int k = 0; k < parts.K; ++k)
+            for_records<REC>(rec, s_lo[k], s_hi[k], vec, [&](uint32_t s, uint32_t d, uint32_t) {
+                atomicAdd(&s_cnt[(key_is_src ? s : d) - v0], 1u);
+            });
         __syncthreads();
         // degrees out, then offsets from the block scan
         for (uint32_t i = threadIdx.x; i < nv; i += blockDim.x) deg[v0 + i] = s_cnt[i];
@@ -561,11 +589,12 @@ __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* _
         for (uint32_t i = threadIdx.x; i < nv; i += blockDim.x) off[v0 + i] = r0 + s_cnt[i];
         if (threadIdx.x == 0 && v0 + nv == V) off[V] = r1;
         __syncthreads();
-        for_records<REC>(rec, r0, r1, vec, [&](uint32_t s, uint32_t d, uint32_t wb) {
-            const uint64_t pos = r0 + atomicAdd(&s_cnt[(key_is_src ? s : d) - v0], 1u);
-            st_keep_u32(adj + pos, key_is_src ? d : s, keep);
-            if (REC == 12) st_keep_u32(reinterpret_cast<uint32_t*>(wout) + pos, wb, keep);
-        });
+        for (int k = 0; k < parts.K; ++k)
+            for_records<REC>(rec, s_lo[k], s_hi[k], vec, [&](uint32_t s, uint32_t d, uint32_t wb) {
+                const uint64_t pos = r0 + atomicAdd(&s_cnt[(key_is_src ? s : d) - v0], 1u);
+                st_keep_u32(adj + pos, key_is_src ? d : s, keep);
+                if (REC == 12) st_keep_u32(reinterpret_cast<uint32_t*>(wout) + pos, wb, keep);
+            });
         __syncthreads();
     }
 }
@@ -594,7 +623,10 @@ static BucketPlan plan_buckets(uint32_t V, uint64_t E) {
 
 int scan_exclusive_u32(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out);
 
-static int build_single(eg_graph* g, int want_csr, int want_csc) {
+// up (optional): the records are still being uploaded in parts; part k may be read once up->ready[k]
+// has completed.  Passes A and B of each part run as soon as it lands (so the upload of the next
+// parts overlaps them) and validate the ids on the way; pass C needs every part.
+static int build_single(eg_graph* g, const UploadParts* up) {
     const uint32_t V = g->V;
     const uint64_t E = g->E;
     const int rec = g->edge_bytes;
@@ -615,71 +647,109 @@ static int build_single(eg_graph* g, int want_csr, int want_csc) {
         EG_CUDA(cudaMemsetAsync(g->csc_off.ptr, 0, sizeof(uint64_t) * ((size_t)V + 1), g->stream));
         return EG_OK;
     }
-    const BucketPlan pl = plan_buckets(V, E);
-    const uint64_t ncnt = 2ull * pl.nb * pl.nblk;
-    EG_TRY(g->bucket_cnt.reserve(sizeof(uint32_t) * ncnt));
-    EG_TRY(g->bucket_off.reserve(sizeof(uint64_t) * (ncnt + 1)));
+    const int K = up ? up->K : 1;
+    std::vector<uint64_t> e0(K + 1, 0);
+    for (int k = 0; k <= K; ++k) e0[k] = up ? up->e0[k] : (k ? E : 0);
+    std::vector<BucketPlan> pl(K);
+    std::vector<uint64_t> co(K + 1, 0), oo(K + 1, 0);  // count / offset table positions per part
+    for (int k = 0; k < K; ++k) {
+        pl[k] = plan_buckets(V, e0[k + 1] - e0[k]);
+        co[k + 1] = co[k] + 2ull * pl[k].nb * pl[k].nblk;
+        oo[k + 1] = oo[k] + 2ull * pl[k].nb * pl[k].nblk + 1;
+    }
+    const uint32_t nb = pl[0].nb, LB = pl[0].LB;
+    const int shift = pl[0].shift;
+    EG_TRY(g->bucket_cnt.reserve(sizeof(uint32_t) * co[K]));
+    EG_TRY(g->bucket_off.reserve(sizeof(uint64_t) * oo[K]));
     EG_TRY(g->bucketed.reserve((size_t)2 * E * rec + 64));
     EG_TRY(g->scan.counter.reserve(16));
-    {
-        Timed t(&g->prof, g->stream, "bucket_hist");
-        size_t smem = sizeof(uint32_t) * 2 * pl.nb;
-        if (rec == 8) {
-            EG_CUDA(cudaFuncSetAttribute(k_bucket_hist<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_bucket_hist<8><<<pl.nblk, kBucketThreads, smem, g->stream>>>(g->edges.as<uint8_t>(), E, pl.chunk, pl.shift,
-                                                                            pl.nb, pl.nblk, g->bucket_cnt.as<uint32_t>());
-        } else {
-            EG_CUDA(cudaFuncSetAttribute(k_bucket_hist<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_bucket_hist<12><<<pl.nblk, kBucketThreads, smem, g->stream>>>(g->edges.as<uint8_t>(), E, pl.chunk, pl.shift,
-                                                                             pl.nb, pl.nblk, g->bucket_cnt.as<uint32_t>());
+    int* bad = g->err.as<int>() + 1;
+    EG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), g->stream));
+    const size_t smem_a = sizeof(uint32_t) * 2 * nb;
+    const size_t smem_b = align16(20ull * nb) + (size_t)scatter_tile(rec) * rec;  // [2][nb] u64, [nb] u32, tile
+    auto scatter_fn = [&]() -> const void* {
+        if (rec == 8) return up ? (const void*)k_bucket_scatter<8, true> : (const void*)k_bucket_scatter<8, false>;
+        return up ? (const void*)k_bucket_scatter<12, true> : (const void*)k_bucket_scatter<12, false>;
+    };
+    EG_CUDA(cudaFuncSetAttribute(scatter_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b));
+    if (rec == 8)
+        EG_CUDA(cudaFuncSetAttribute(k_bucket_hist<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a));
+    else
+        EG_CUDA(cudaFuncSetAttribute(k_bucket_hist<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a));
+    BuildParts parts{};
+    parts.K = K;
+    for (int k = 0; k < K; ++k) {
+        if (up) EG_CUDA(cudaStreamWaitEvent(g->stream, up->ready[k], 0));
+        const uint64_t Ek = e0[k + 1] - e0[k];
+        const uint8_t* src = g->edges.as<uint8_t>() + (size_t)e0[k] * rec;
+        uint32_t* cnt = g->bucket_cnt.as<uint32_t>() + co[k];
+        uint64_t* ex = g->bucket_off.as<uint64_t>() + oo[k];
+        uint8_t* out = g->bucketed.as<uint8_t>() + (size_t)2 * e0[k] * rec;
+        const BucketPlan& q = pl[k];
+        {
+            Timed t(&g->prof, g->stream, "bucket_hist");
+            if (rec == 8)
+                k_bucket_hist<8><<<q.nblk, kBucketThreads, smem_a, g->stream>>>(src, Ek, q.chunk, shift, nb, q.nblk, cnt,
+                                                                                 V, bad);
+            else
+                k_bucket_hist<12><<<q.nblk, kBucketThreads, smem_a, g->stream>>>(src, Ek, q.chunk, shift, nb, q.nblk,
+                                                                                  cnt, V, bad);
+            EG_CHECK_LAUNCH("k_bucket_hist");
         }
-        EG_CHECK_LAUNCH("k_bucket_hist");
-    }
-    EG_TRY(scan_exclusive_u32(g, g->bucket_cnt.as<uint32_t>(), ncnt, g->bucket_off.as<uint64_t>()));
-    {
-        Timed t(&g->prof, g->stream, "bucket_scatter");
-        size_t smem = align16(20ull * pl.nb) + (size_t)scatter_tile(rec) * rec;  // [2][nb] u64, [nb] u32, tile
-        if (rec == 8) {
-            EG_CUDA(cudaFuncSetAttribute(k_bucket_scatter<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_bucket_scatter<8><<<pl.nblk, kScatterThreads, smem, g->stream>>>(
-                g->edges.as<uint8_t>(), E, pl.chunk, pl.shift, pl.nb, pl.nblk, g->bucket_off.as<uint64_t>(),
-                g->bucketed.as<uint8_t>());
-        } else {
-            EG_CUDA(cudaFuncSetAttribute(k_bucket_scatter<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_bucket_scatter<12><<<pl.nblk, kScatterThreads, smem, g->stream>>>(
-                g->edges.as<uint8_t>(), E, pl.chunk, pl.shift, pl.nb, pl.nblk, g->bucket_off.as<uint64_t>(),
-                g->bucketed.as<uint8_t>());
+        EG_TRY(scan_exclusive_u32(g, cnt, co[k + 1] - co[k], ex));
+        {
+            Timed t(&g->prof, g->stream, "bucket_scatter");
+            if (rec == 8 && up)
+                k_bucket_scatter<8, true><<<q.nblk, kScatterThreads, smem_b, g->stream>>>(src, Ek, q.chunk, shift, nb,
+                                                                                          q.nblk, ex, out, V);
+            else if (rec == 8)
+                k_bucket_scatter<8, false><<<q.nblk, kScatterThreads, smem_b, g->stream>>>(src, Ek, q.chunk, shift, nb,
+                                                                                           q.nblk, ex, out, V);
+            else if (up)
+                k_bucket_scatter<12, true><<<q.nblk, kScatterThreads, smem_b, g->stream>>>(src, Ek, q.chunk, shift, nb,
+                                                                                           q.nblk, ex, out, V);
+            else
+                k_bucket_scatter<12, false><<<q.nblk, kScatterThreads, smem_b, g->stream>>>(src, Ek, q.chunk, shift,
+                                                                                            nb, q.nblk, ex, out, V);
+            EG_CHECK_LAUNCH("k_bucket_scatter");
         }
-        EG_CHECK_LAUNCH("k_bucket_scatter");
+        parts.base2[k] = 2 * e0[k];
+        parts.excl[k] = ex;
+        parts.nblk[k] = q.nblk;
     }
-    const size_t smem_c = sizeof(uint32_t) * pl.LB;
+    if (up) {  // an upload validates in pass A: ids >= V stop the build here
+        int h = 0;
+        EG_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaStreamSynchronize(g->stream));
+        if (h) {
+            set_error("edge list holds a vertex id >= V (%u)", V);
+            return EG_ERR_INVALID;
+        }
+    }
+    const size_t smem_c = sizeof(uint32_t) * LB;
     if (rec == 8) EG_CUDA(cudaFuncSetAttribute(k_bucket_build<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
     else EG_CUDA(cudaFuncSetAttribute(k_bucket_build<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
+    int per_sm = 1;
+    if (rec == 8)
+        EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bucket_build<8>, kBuildThreads, smem_c));
+    else
+        EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bucket_build<12>, kBuildThreads, smem_c));
+    const unsigned grid = std::min<uint32_t>(nb, (uint32_t)g->num_sms * (uint32_t)std::max(per_sm, 1));
     for (int half = 0; half < 2; ++half) {
         EG_CUDA(cudaMemsetAsync(g->scan.counter.ptr, 0, 4, g->stream));
         Timed t(&g->prof, g->stream, "bucket_build");
-        const uint8_t* recs = g->bucketed.as<uint8_t>() + (size_t)half * E * rec;
-        const uint64_t* ex = g->bucket_off.as<uint64_t>() + (size_t)half * pl.nb * pl.nblk;
         uint32_t* deg = half == 0 ? g->outdeg.as<uint32_t>() : g->indeg.as<uint32_t>();
         uint64_t* off = half == 0 ? g->csr_off.as<uint64_t>() : g->csc_off.as<uint64_t>();
         uint32_t* adj = half == 0 ? g->csr_adj.as<uint32_t>() : g->csc_adj.as<uint32_t>();
         float* w = half == 0 ? g->csr_w.as<float>() : g->csc_w.as<float>();
-        int per_sm = 1;
         if (rec == 8)
-            EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bucket_build<8>, kBuildThreads, smem_c));
+            k_bucket_build<8><<<grid, kBuildThreads, smem_c, g->stream>>>(g->bucketed.as<uint8_t>(), parts, half, nb, LB,
+                                                                          V, deg, off, adj, w,
+                                                                          g->scan.counter.as<uint32_t>());
         else
-            EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bucket_build<12>, kBuildThreads, smem_c));
-        unsigned grid = std::min<uint32_t>(pl.nb, (uint32_t)g->num_sms * (uint32_t)std::max(per_sm, 1));
-        if (rec == 8) {
-            k_bucket_build<8><<<grid, kBuildThreads, smem_c, g->stream>>>(recs, ex, (uint64_t)half * E, E, pl.nb, pl.nblk,
-                                                                          pl.LB, V, half == 0, deg, off, adj, w,
-                                                                          g->scan.counter.as<uint32_t>(),
-                                                                          ((uintptr_t)recs & 15u) == 0);
-        } else {
-            k_bucket_build<12><<<grid, kBuildThreads, smem_c, g->stream>>>(recs, ex, (uint64_t)half * E, E, pl.nb, pl.nblk,
-                                                                           pl.LB, V, half == 0, deg, off, adj, w,
-                                                                           g->scan.counter.as<uint32_t>(), 0);
-        }
+            k_bucket_build<12><<<grid, kBuildThreads, smem_c, g->stream>>>(g->bucketed.as<uint8_t>(), parts, half, nb,
+                                                                           LB, V, deg, off, adj, w,
+                                                                           g->scan.counter.as<uint32_t>());
         EG_CHECK_LAUNCH("k_bucket_build");
     }
     return EG_OK;
@@ -797,7 +867,7 @@ int cpbt_device(eg_graph* g, const uint32_t* d_deg, uint32_t V, int P, int S, ui
     return EG_OK;
 }
 
-int build_structures(eg_graph* g, int want_csr, int want_csc) {
+int build_structures(eg_graph* g, int want_csr, int want_csc, const UploadParts* up) {
     const uint32_t V = g->V;
     const uint64_t E = g->E;
     const int P = g->partitions, S = g->sub_partitions;
@@ -814,8 +884,12 @@ int build_structures(eg_graph* g, int want_csr, int want_csc) {
     if (bucketed) {
         // one partition: both structures (and both degree arrays) from the bucketed build
         want_csr = want_csc = 1;
-        EG_TRY(build_single(g, 1, 1));
+        EG_TRY(build_single(g, up));
     } else {
+        if (up) {  // the generic path reads the whole list: wait for every part
+            for (int k = 0; k < up->K; ++k) EG_CUDA(cudaStreamWaitEvent(g->stream, up->ready[k], 0));
+            EG_TRY(validate_edges(g, E));
+        }
         EG_TRY(compute_degrees(g));
     }
     // assign_vertices: dense (out-degree) weights with T = max_iterations

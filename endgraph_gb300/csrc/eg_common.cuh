@@ -171,6 +171,10 @@ struct eg_graph {
     // pinned staging for host inputs
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
+    // pipelined host loads: the upload stream, its per-part events and the gate on prior work
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t part_ready[8] = {};
+    cudaEvent_t copy_gate = nullptr;
     // batched operators (eg_batch.cu): opaque state, dropped at every load/build
     void* batch = nullptr;
     bool edge_ids = false;   // the weight slot of each record holds the record's input index
@@ -198,7 +202,17 @@ namespace eg {
 int scan_u32_to_u64(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out_incl, uint64_t* total_dev);
 int compress_index(eg_graph* g, const uint32_t* cnt, uint64_t n, uint32_t V, const uint64_t* off,
                    uint32_t* cvert, uint64_t* cidx, uint64_t* count_dev);
-int build_structures(eg_graph* g, int want_csr, int want_csc);
+// records uploaded in parts on another stream: part k = records [e0[k], e0[k+1]) is resident once
+// ready[k] has completed
+struct UploadParts {
+    int K;
+    uint64_t e0[9];
+    cudaEvent_t ready[8];
+};
+int build_structures(eg_graph* g, int want_csr, int want_csc, const UploadParts* up = nullptr);
+// eg_load_directed of host records from this many records on: upload and build pipelined
+constexpr uint64_t kPipelinedLoadMin = 1ull << 22;
+int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes);
 int compute_degrees(eg_graph* g);
 int cpbt_device(eg_graph* g, const uint32_t* d_deg, uint32_t V, int P, int S, uint64_t eta, int T, int dense,
                 uint32_t* h_part, uint32_t* h_local);

@@ -1,11 +1,12 @@
 """Edge cases through the C ABI against the oracle: empty and one-vertex graphs, self loops and
 duplicate edges, a hub whose in-list is long enough for the segmented dense BFS step, a path deeper
-than the captured MS-BFS loop, ids out of range, and more partitions than CPBT pages."""
+than the captured MS-BFS loop, ids out of range, the pipelined upload of large host edge lists, and
+more partitions than CPBT pages."""
 import numpy as np
 import pytest
 
 import oracle
-from helpers import lists_equal, rel_l1
+from helpers import lists_equal, rel_l1, rmat_graph
 
 pytestmark = pytest.mark.gpu
 
@@ -108,6 +109,41 @@ def test_ids_out_of_range_are_rejected(eg_lib):
         g.load_directed(eg.pack_edges(np.array([0, 4], np.uint32), np.array([1, 2], np.uint32)), 5)
         lv, _ = g.bfs(0)
         assert list(lv[:2]) == [0, 1]
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_pipelined_host_load_matches_device_load(eg_lib, weighted):
+    """eg_load_directed of host records with >= 2^22 edges uploads in parts and builds each part
+    as it lands (ids validated in the first pass): the same degrees, CSR, CSC, compressed index and
+    PageRank as loading the records first and building after, for a ragged last part; an id >= V
+    in the last part is rejected and the handle stays usable."""
+    import torch
+
+    import endgraph_gb300 as eg
+    V, E = 1 << 18, (1 << 22) + 12_345
+    src, dst, w = rmat_graph(V, E, 123, weights=(0.0, 1.0) if weighted else None)
+    rec = eg.pack_edges(src, dst, w)
+    with eg.Graph() as a, eg.Graph() as b:
+        a.load_directed(rec, V)  # host records: pipelined upload + build
+        dev = torch.from_numpy(rec.view(np.int32)).cuda()
+        b.load_edges(dev, V)  # device records, loaded then built
+        b.build()
+        assert np.array_equal(a.degrees()[0], b.degrees()[0]) and np.array_equal(a.degrees()[1], b.degrees()[1])
+        ca, cb = a.csr(), b.csr()
+        assert lists_equal(ca["off"][0], ca["adj"], cb["off"][0], cb["adj"], ca["w"], cb["w"])
+        assert np.array_equal(ca["bitmap"], cb["bitmap"])
+        ka, kb = a.csc(), b.csc()
+        assert lists_equal(ka["off"][0], ka["adj"], kb["off"][0], kb["adj"], ka["w"], kb["w"])
+        assert np.array_equal(ka["cvert"], kb["cvert"]) and np.array_equal(ka["cidx"], kb["cidx"])
+        o_out, _ = oracle.degrees(src, dst, V)
+        assert np.array_equal(a.degrees()[0], o_out)
+        assert rel_l1(a.pagerank(20, 0.85), b.pagerank(20, 0.85)) <= 1e-6
+        bad = rec.copy()
+        bad[E - 3, 1] = V  # a destination id out of range in the last part
+        with pytest.raises(eg.EndGraphError):
+            a.load_directed(bad, V)
+        a.load_directed(rec, V)
+        assert np.array_equal(a.degrees()[1], b.degrees()[1])
 
 
 def test_more_partitions_than_pages(eg_lib):
