@@ -6,7 +6,9 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <condition_variable>
 #include <memory>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -259,10 +261,90 @@ static int prepare_load(eg_graph* g, uint64_t E, uint32_t V, int edge_bytes, int
     return EG_OK;
 }
 
-// preload_graph_file (core/graph.hpp:1011-1084) for one rank: the whole file, read in 64 MiB
+// preload_graph_file (core/graph.hpp:1011-1084) for one rank: the whole file, read in 128 MiB
 // pieces into two pinned staging buffers, so that reading piece i+1 overlaps the host-to-device
 // copy of piece i; then the same validation and symmetrisation as eg_load_edges.
-constexpr size_t kIngestPiece = 64ull << 20;
+constexpr size_t kIngestPiece = 128ull << 20;
+
+// Reader threads started once per file: each piece is split into one slice per thread (page-cache
+// copies are bound per thread), and the caller waits until every slice of the piece is in.
+class ReaderPool {
+   public:
+    ReaderPool(int fd, unsigned nt) : fd_(fd), nt_(nt) {
+        for (unsigned t = 0; t < nt; ++t) threads_.emplace_back([this, t] { run(t); });
+    }
+    ~ReaderPool() {
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            stop_ = true;
+            ++gen_;
+        }
+        cv_.notify_all();
+        for (auto& th : threads_) th.join();
+    }
+    // bytes [off, off + n) of the file into buf; false on a short read
+    bool read(uint8_t* buf, uint64_t off, size_t n) {
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            buf_ = buf;
+            off_ = off;
+            n_ = n;
+            pending_ = nt_;
+            ok_ = true;
+            ++gen_;
+        }
+        cv_.notify_all();
+        std::unique_lock<std::mutex> lk(m_);
+        done_.wait(lk, [&] { return pending_ == 0; });
+        return ok_;
+    }
+
+   private:
+    void run(unsigned t) {
+        uint64_t seen = 0;
+        while (true) {
+            uint8_t* buf;
+            uint64_t off;
+            size_t n;
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                cv_.wait(lk, [&] { return gen_ != seen; });
+                seen = gen_;
+                if (stop_) return;
+                buf = buf_;
+                off = off_;
+                n = n_;
+            }
+            const size_t part = (n + nt_ - 1) / nt_;
+            const size_t a = std::min(n, t * part), z = std::min(n, a + part);
+            size_t got = 0;
+            bool good = true;
+            while (a + got < z) {
+                const ssize_t r = pread(fd_, buf + a + got, z - a - got, (off_t)(off + a + got));
+                if (r < 0 && errno == EINTR) continue;
+                if (r <= 0) {
+                    good = false;
+                    break;
+                }
+                got += (size_t)r;
+            }
+            std::lock_guard<std::mutex> lk(m_);
+            if (!good) ok_ = false;
+            if (--pending_ == 0) done_.notify_one();
+        }
+    }
+    int fd_;
+    unsigned nt_;
+    std::vector<std::thread> threads_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    uint64_t gen_ = 0;
+    bool stop_ = false, ok_ = true;
+    unsigned pending_ = 0;
+    uint8_t* buf_ = nullptr;
+    uint64_t off_ = 0;
+    size_t n_ = 0;
+};
 
 int load_file_impl(eg_graph* g, const char* path, uint32_t V, int edge_bytes, int symmetric) {
     if (!path) {
@@ -312,6 +394,7 @@ int load_file_impl(eg_graph* g, const char* path, uint32_t V, int edge_bytes, in
         if (e != cudaSuccess) status = cuda_fail(e, "cudaEventCreate", __FILE__, __LINE__);
     }
     uint8_t* dst = g->edges.as<uint8_t>();
+    ReaderPool pool(fd, std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
     for (uint64_t off = 0, piece = 0; status == EG_OK && off < bytes; off += kIngestPiece, ++piece) {
         const int slot = (int)(piece & 1);
         uint8_t* buf = static_cast<uint8_t*>(g->pinned) + slot * kIngestPiece;
@@ -323,28 +406,7 @@ int load_file_impl(eg_graph* g, const char* path, uint32_t V, int edge_bytes, in
             }
         }
         const size_t n = (size_t)std::min<uint64_t>(kIngestPiece, bytes - off);
-        // the piece is read by several threads at once (page-cache copies are per-thread bound)
-        const unsigned nt = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
-        const size_t part = (n + nt - 1) / nt;
-        std::vector<size_t> got(nt, 0);
-        std::vector<std::thread> readers;
-        for (unsigned t = 0; t < nt; ++t) {
-            const size_t a = std::min(n, t * part), z = std::min(n, a + part);
-            readers.emplace_back([&, t, a, z]() {
-                size_t done_t = 0;
-                while (a + done_t < z) {
-                    const ssize_t r = pread(fd, buf + a + done_t, z - a - done_t, (off_t)(off + a + done_t));
-                    if (r < 0 && errno == EINTR) continue;
-                    if (r <= 0) break;
-                    done_t += (size_t)r;
-                }
-                got[t] = (a + done_t == z) ? 1 : 0;
-            });
-        }
-        for (auto& th : readers) th.join();
-        bool whole = true;
-        for (unsigned t = 0; t < nt; ++t) whole = whole && got[t];
-        if (!whole) {
+        if (!pool.read(buf, off, n)) {
             set_error("eg_load_file: short read of %s in the piece at byte %llu", path, (unsigned long long)off);
             status = EG_ERR_INVALID;
             break;
