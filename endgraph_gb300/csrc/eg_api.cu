@@ -202,10 +202,19 @@ int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V,
     for (cudaEvent_t& e : g->part_ready)
         if (!e) EG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     UploadParts up{};
-    up.K = (int)std::max<uint64_t>(1, std::min<uint64_t>(8, E / (kPipelinedLoadMin / 2)));
-    const uint64_t per = ((E + up.K - 1) / up.K + 63) & ~63ull;  // parts start on 64-record boundaries
+    const int want = (int)std::max<uint64_t>(1, std::min<uint64_t>(8, E / (kPipelinedLoadMin / 2)));
+    // the last part's passes follow the copy, so it is the smallest (1/32 of the records); the
+    // others share the rest; parts start on 64-record boundaries
+    const uint64_t last = want > 1 ? E / 32 : 0;
+    const uint64_t per = want > 1 ? ((E - last + want - 2) / (want - 1) + 63) & ~63ull : E;
     int K = 0;
-    for (uint64_t a = 0; a < E && K < 8; a += per) up.e0[K++] = a;
+    for (uint64_t a = 0; a < E && K < want - 1; a += per) up.e0[K++] = a;
+    if (want > 1) {
+        const uint64_t tail = (E - last) & ~63ull;
+        if (K == 0 || tail > up.e0[K - 1]) up.e0[K++] = tail;
+    } else if (K == 0) {
+        up.e0[K++] = 0;
+    }
     up.K = K;
     up.e0[K] = E;
     // the records buffer may still be read by earlier work on the handle's stream
