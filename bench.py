@@ -540,14 +540,18 @@ def run_ours(args, world, rank, local):
         n_e2e = max(2, min(args.steps, 5))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        marks = []
         for _ in range(n_e2e):
             g2.load_directed(h_np, V)
             po, _ = g2.partition()
+            marks.append(time.perf_counter())
         g2.sync()
         e2e_s = (time.perf_counter() - t0) / n_e2e
         e2e_s = max_over_ranks(e2e_s, world, dev)
         e2e = {"value": round(world * E / e2e_s / 1e6, 3), "unit": "Medges/s", "h2d_bytes_per_step": 8 * E,
                "d2h_bytes_per_step": 4 * len(po) + 64, "ms_per_step": round(e2e_s * 1e3, 3),
+               "per_step_ms": [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)],
+               "host_pinned": bool(host.is_pinned()),
                "path": "eg_load_directed(host pinned records) + eg_get_partition"}
         # the same through the reference's input path: the binary edge file, streamed through
         # pinned staging buffers (eg_load_file); the file sits in the page cache after writing

@@ -191,53 +191,6 @@ int load_edges_impl(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int 
     return EG_OK;
 }
 
-// Host records uploaded in up to 8 parts on the handle's copy stream while the build consumes
-// them: passes A and B of part k (and the id validation, in pass A) run on the handle's stream as
-// soon as part k has landed, so only the last part's passes and pass C follow the upload.  The
-// caller's buffer is read until this returns.
-int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes) {
-    EG_TRY(prepare_load(g, E, V, edge_bytes, 0));
-    if (!g->copy_stream) EG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
-    if (!g->copy_gate) EG_CUDA(cudaEventCreateWithFlags(&g->copy_gate, cudaEventDisableTiming));
-    for (cudaEvent_t& e : g->part_ready)
-        if (!e) EG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    UploadParts up{};
-    const int want = (int)std::max<uint64_t>(1, std::min<uint64_t>(8, E / (kPipelinedLoadMin / 2)));
-    // the last part's passes follow the copy, so it is the smallest (1/32 of the records); the
-    // others share the rest; parts start on 64-record boundaries
-    const uint64_t last = want > 1 ? E / 32 : 0;
-    const uint64_t per = want > 1 ? ((E - last + want - 2) / (want - 1) + 63) & ~63ull : E;
-    int K = 0;
-    for (uint64_t a = 0; a < E && K < want - 1; a += per) up.e0[K++] = a;
-    if (want > 1) {
-        const uint64_t tail = (E - last) & ~63ull;
-        if (K == 0 || tail > up.e0[K - 1]) up.e0[K++] = tail;
-    } else if (K == 0) {
-        up.e0[K++] = 0;
-    }
-    up.K = K;
-    up.e0[K] = E;
-    // the records buffer may still be read by earlier work on the handle's stream
-    EG_CUDA(cudaEventRecord(g->copy_gate, g->stream));
-    EG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->copy_gate, 0));
-    const uint8_t* src = static_cast<const uint8_t*>(edges);
-    for (int k = 0; k < K; ++k) {
-        const size_t off = (size_t)up.e0[k] * edge_bytes, n = (size_t)(up.e0[k + 1] - up.e0[k]) * edge_bytes;
-        EG_CUDA(cudaMemcpyAsync(g->edges.as<uint8_t>() + off, src + off, n, cudaMemcpyHostToDevice, g->copy_stream));
-        EG_CUDA(cudaEventRecord(g->part_ready[k], g->copy_stream));
-        up.ready[k] = g->part_ready[k];
-    }
-    free_batch_state(g);
-    const int st = build_structures(g, 1, 1, &up);
-    const cudaError_t e = cudaStreamSynchronize(g->copy_stream);  // never return with the buffer in use
-    if (st != EG_OK) {
-        g->V = 0;  // no usable edge list
-        return st;
-    }
-    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
-    return EG_OK;
-}
-
 // argument checks, state reset and the record buffer of a new edge list
 static int prepare_load(eg_graph* g, uint64_t E, uint32_t V, int edge_bytes, int symmetric) {
     if (edge_bytes != 8 && edge_bytes != 12) {
@@ -275,11 +228,12 @@ static int prepare_load(eg_graph* g, uint64_t E, uint32_t V, int edge_bytes, int
 // copy of piece i; then the same validation and symmetrisation as eg_load_edges.
 constexpr size_t kIngestPiece = 128ull << 20;
 
-// Reader threads started once per file: each piece is split into one slice per thread (page-cache
-// copies are bound per thread), and the caller waits until every slice of the piece is in.
+// Reader threads started once per file (or per host buffer, mem != null): each piece is split into
+// one slice per thread (page-cache and pageable-memory copies are bound per thread), and the caller
+// waits until every slice of the piece is in.
 class ReaderPool {
    public:
-    ReaderPool(int fd, unsigned nt) : fd_(fd), nt_(nt) {
+    ReaderPool(int fd, unsigned nt, const uint8_t* mem = nullptr) : fd_(fd), nt_(nt), mem_(mem) {
         for (unsigned t = 0; t < nt; ++t) threads_.emplace_back([this, t] { run(t); });
     }
     ~ReaderPool() {
@@ -328,6 +282,10 @@ class ReaderPool {
             const size_t a = std::min(n, t * part), z = std::min(n, a + part);
             size_t got = 0;
             bool good = true;
+            if (mem_) {
+                memcpy(buf + a, mem_ + off + a, z - a);
+                got = z - a;
+            }
             while (a + got < z) {
                 const ssize_t r = pread(fd_, buf + a + got, z - a - got, (off_t)(off + a + got));
                 if (r < 0 && errno == EINTR) continue;
@@ -344,6 +302,7 @@ class ReaderPool {
     }
     int fd_;
     unsigned nt_;
+    const uint8_t* mem_;
     std::vector<std::thread> threads_;
     std::mutex m_;
     std::condition_variable cv_, done_;
@@ -354,6 +313,120 @@ class ReaderPool {
     uint64_t off_ = 0;
     size_t n_ = 0;
 };
+
+// the two pinned staging buffers of file reads and pageable uploads
+static int ensure_staging(eg_graph* g) {
+    if (g->pinned_bytes >= 2 * kIngestPiece) return EG_OK;
+    if (g->pinned) cudaFreeHost(g->pinned);
+    g->pinned = nullptr;
+    g->pinned_bytes = 0;
+    cudaError_t e = cudaHostAlloc(&g->pinned, 2 * kIngestPiece, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        g->pinned = nullptr;
+        return cuda_fail(e, "cudaHostAlloc", __FILE__, __LINE__);
+    }
+    g->pinned_bytes = 2 * kIngestPiece;
+    return EG_OK;
+}
+
+// Host records uploaded in up to 8 parts on the handle's copy stream while the build consumes
+// them: passes A and B of part k (and the id validation, in pass A) run on the handle's stream as
+// soon as part k has landed, so only the last part's passes and pass C follow the upload.  The
+// caller's buffer is read until this returns.
+int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes) {
+    EG_TRY(prepare_load(g, E, V, edge_bytes, 0));
+    if (!g->copy_stream) EG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    if (!g->copy_gate) EG_CUDA(cudaEventCreateWithFlags(&g->copy_gate, cudaEventDisableTiming));
+    for (cudaEvent_t& e : g->part_ready)
+        if (!e) EG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    UploadParts up{};
+    const int want = (int)std::max<uint64_t>(1, std::min<uint64_t>(8, E / (kPipelinedLoadMin / 2)));
+    // the last part's passes follow the copy, so it is the smallest (1/32 of the records); the
+    // others share the rest; parts start on 64-record boundaries
+    const uint64_t last = want > 1 ? E / 32 : 0;
+    const uint64_t per = want > 1 ? ((E - last + want - 2) / (want - 1) + 63) & ~63ull : E;
+    int K = 0;
+    for (uint64_t a = 0; a < E && K < want - 1; a += per) up.e0[K++] = a;
+    if (want > 1) {
+        const uint64_t tail = (E - last) & ~63ull;
+        if (K == 0 || tail > up.e0[K - 1]) up.e0[K++] = tail;
+    } else if (K == 0) {
+        up.e0[K++] = 0;
+    }
+    up.K = K;
+    up.e0[K] = E;
+    // the records buffer may still be read by earlier work on the handle's stream
+    EG_CUDA(cudaEventRecord(g->copy_gate, g->stream));
+    EG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->copy_gate, 0));
+    const uint8_t* src = static_cast<const uint8_t*>(edges);
+    for (int k = 0; k < K; ++k) up.ready[k] = g->part_ready[k];
+    cudaPointerAttributes attr{};
+    const bool pinned = cudaPointerGetAttributes(&attr, edges) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+    cudaGetLastError();  // a pageable pointer may leave an error behind on older drivers
+    free_batch_state(g);
+    if (pinned) {  // the copy engines read the caller's buffer directly: every part queued now
+        for (int k = 0; k < K; ++k) {
+            const size_t off = (size_t)up.e0[k] * edge_bytes, n = (size_t)(up.e0[k + 1] - up.e0[k]) * edge_bytes;
+            EG_CUDA(cudaMemcpyAsync(g->edges.as<uint8_t>() + off, src + off, n, cudaMemcpyHostToDevice, g->copy_stream));
+            EG_CUDA(cudaEventRecord(g->part_ready[k], g->copy_stream));
+        }
+        const int st = build_structures(g, 1, 1, &up);
+        const cudaError_t e = cudaStreamSynchronize(g->copy_stream);  // never return with the buffer in use
+        if (st != EG_OK) {
+            g->V = 0;  // no usable edge list
+            return st;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+        return EG_OK;
+    }
+    // pageable memory: a staging thread copies each part through the two pinned buffers (host
+    // threads memcpy a piece while the previous piece goes up) and records the part's event; the
+    // build waits for each event only after it has been recorded
+    EG_TRY(ensure_staging(g));
+    std::atomic<int> issued{0};
+    std::atomic<bool> failed{false};
+    up.issued = &issued;
+    up.failed = &failed;
+    cudaError_t stage_err = cudaSuccess;
+    std::thread stager([&]() {
+        cudaSetDevice(g->device);
+        cudaEvent_t done[2] = {nullptr, nullptr};
+        cudaError_t e = cudaSuccess;
+        for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
+        ReaderPool pool(-1, std::max(1u, std::min(16u, std::thread::hardware_concurrency())), src);
+        uint64_t piece = 0;
+        for (int k = 0; k < K && e == cudaSuccess; ++k) {
+            const uint64_t a = up.e0[k] * (uint64_t)edge_bytes, z = up.e0[k + 1] * (uint64_t)edge_bytes;
+            for (uint64_t off = a; off < z && e == cudaSuccess; off += kIngestPiece, ++piece) {
+                const int slot = (int)(piece & 1);
+                uint8_t* buf = static_cast<uint8_t*>(g->pinned) + slot * kIngestPiece;
+                if (piece >= 2) e = cudaEventSynchronize(done[slot]);  // the copy that last used it
+                if (e != cudaSuccess) break;
+                const size_t n = (size_t)std::min<uint64_t>(kIngestPiece, z - off);
+                pool.read(buf, off, n);
+                e = cudaMemcpyAsync(g->edges.as<uint8_t>() + off, buf, n, cudaMemcpyHostToDevice, g->copy_stream);
+                if (e == cudaSuccess) e = cudaEventRecord(done[slot], g->copy_stream);
+            }
+            if (e == cudaSuccess) e = cudaEventRecord(g->part_ready[k], g->copy_stream);
+            if (e == cudaSuccess) issued.store(k + 1, std::memory_order_release);
+        }
+        if (e != cudaSuccess) {
+            stage_err = e;
+            failed.store(true, std::memory_order_release);
+        }
+        cudaStreamSynchronize(g->copy_stream);  // the staging buffers are reused by the next call
+        for (int i = 0; i < 2; ++i)
+            if (done[i]) cudaEventDestroy(done[i]);
+    });
+    const int st = build_structures(g, 1, 1, &up);
+    stager.join();
+    if (st != EG_OK || stage_err != cudaSuccess) {
+        g->V = 0;  // no usable edge list
+        if (stage_err != cudaSuccess) return cuda_fail(stage_err, "eg_load_directed upload", __FILE__, __LINE__);
+        return st;
+    }
+    return EG_OK;
+}
 
 int load_file_impl(eg_graph* g, const char* path, uint32_t V, int edge_bytes, int symmetric) {
     if (!path) {
@@ -384,17 +457,12 @@ int load_file_impl(eg_graph* g, const char* path, uint32_t V, int edge_bytes, in
         close(fd);
         return st_load;
     }
-    if (g->pinned_bytes < 2 * kIngestPiece) {
-        if (g->pinned) cudaFreeHost(g->pinned);
-        g->pinned = nullptr;
-        g->pinned_bytes = 0;
-        cudaError_t e = cudaHostAlloc(&g->pinned, 2 * kIngestPiece, cudaHostAllocDefault);
-        if (e != cudaSuccess) {
+    {
+        const int st = ensure_staging(g);
+        if (st != EG_OK) {
             close(fd);
-            g->pinned = nullptr;
-            return cuda_fail(e, "cudaHostAlloc", __FILE__, __LINE__);
+            return st;
         }
-        g->pinned_bytes = 2 * kIngestPiece;
     }
     cudaEvent_t done[2] = {nullptr, nullptr};
     int status = EG_OK;

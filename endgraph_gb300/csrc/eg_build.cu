@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <thread>
 
 #include "eg_common.cuh"
 #include "eg_scan.cuh"
@@ -623,6 +624,21 @@ static BucketPlan plan_buckets(uint32_t V, uint64_t E) {
 
 int scan_exclusive_u32(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out);
 
+// the handle's stream waits for part k of an upload (once the uploader has recorded its event)
+static int wait_upload_part(eg_graph* g, const UploadParts* up, int k) {
+    if (up->issued) {
+        while (up->issued->load(std::memory_order_acquire) <= k) {
+            if (up->failed && up->failed->load(std::memory_order_acquire)) {
+                set_error("eg_load_directed: the upload of part %d stopped", k);
+                return EG_ERR_CUDA;
+            }
+            std::this_thread::yield();
+        }
+    }
+    EG_CUDA(cudaStreamWaitEvent(g->stream, up->ready[k], 0));
+    return EG_OK;
+}
+
 // up (optional): the records are still being uploaded in parts; part k may be read once up->ready[k]
 // has completed.  Passes A and B of each part run as soon as it lands (so the upload of the next
 // parts overlaps them) and validate the ids on the way; pass C needs every part.
@@ -679,7 +695,7 @@ static int build_single(eg_graph* g, const UploadParts* up) {
     BuildParts parts{};
     parts.K = K;
     for (int k = 0; k < K; ++k) {
-        if (up) EG_CUDA(cudaStreamWaitEvent(g->stream, up->ready[k], 0));
+        if (up) EG_TRY(wait_upload_part(g, up, k));
         const uint64_t Ek = e0[k + 1] - e0[k];
         const uint8_t* src = g->edges.as<uint8_t>() + (size_t)e0[k] * rec;
         uint32_t* cnt = g->bucket_cnt.as<uint32_t>() + co[k];
@@ -887,7 +903,7 @@ int build_structures(eg_graph* g, int want_csr, int want_csc, const UploadParts*
         EG_TRY(build_single(g, up));
     } else {
         if (up) {  // the generic path reads the whole list: wait for every part
-            for (int k = 0; k < up->K; ++k) EG_CUDA(cudaStreamWaitEvent(g->stream, up->ready[k], 0));
+            for (int k = 0; k < up->K; ++k) EG_TRY(wait_upload_part(g, up, k));
             EG_TRY(validate_edges(g, E));
         }
         EG_TRY(compute_degrees(g));

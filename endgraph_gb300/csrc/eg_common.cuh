@@ -204,10 +204,14 @@ int compress_index(eg_graph* g, const uint32_t* cnt, uint64_t n, uint32_t V, con
                    uint32_t* cvert, uint64_t* cidx, uint64_t* count_dev);
 // records uploaded in parts on another stream: part k = records [e0[k], e0[k+1]) is resident once
 // ready[k] has completed
+// ready[k]: an upload thread that records the events as it goes publishes how many are recorded
+// in *issued (null: all recorded up front) and raises *failed if it stops early
 struct UploadParts {
     int K;
     uint64_t e0[9];
     cudaEvent_t ready[8];
+    const std::atomic<int>* issued = nullptr;
+    const std::atomic<bool>* failed = nullptr;
 };
 int build_structures(eg_graph* g, int want_csr, int want_csc, const UploadParts* up = nullptr);
 // eg_load_directed of host records from this many records on: upload and build pipelined

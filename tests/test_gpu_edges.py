@@ -111,18 +111,23 @@ def test_ids_out_of_range_are_rejected(eg_lib):
         assert list(lv[:2]) == [0, 1]
 
 
-@pytest.mark.parametrize("weighted", [False, True])
-def test_pipelined_host_load_matches_device_load(eg_lib, weighted):
+@pytest.mark.parametrize("weighted,pinned", [(False, False), (True, False), (False, True)])
+def test_pipelined_host_load_matches_device_load(eg_lib, weighted, pinned):
     """eg_load_directed of host records with >= 2^22 edges uploads in parts and builds each part
-    as it lands (ids validated in the first pass): the same degrees, CSR, CSC, compressed index and
-    PageRank as loading the records first and building after, for a ragged last part; an id >= V
-    in the last part is rejected and the handle stays usable."""
+    as it lands (ids validated in the first pass), from pinned memory directly or from pageable
+    memory through the staging buffers: the same degrees, CSR, CSC, compressed index and PageRank
+    as loading the records first and building after, for a ragged last part; an id >= V in the
+    last part is rejected and the handle stays usable."""
     import torch
 
     import endgraph_gb300 as eg
     V, E = 1 << 18, (1 << 22) + 12_345
     src, dst, w = rmat_graph(V, E, 123, weights=(0.0, 1.0) if weighted else None)
     rec = eg.pack_edges(src, dst, w)
+    if pinned:
+        host = torch.empty(rec.shape, dtype=torch.int32, pin_memory=True)
+        host.numpy()[:] = rec.view(np.int32)
+        rec = host.numpy().view(np.uint32)
     with eg.Graph() as a, eg.Graph() as b:
         a.load_directed(rec, V)  # host records: pipelined upload + build
         dev = torch.from_numpy(rec.view(np.int32)).cuda()
