@@ -548,10 +548,19 @@ def run_ours(args, world, rank, local):
         g2.sync()
         e2e_s = (time.perf_counter() - t0) / n_e2e
         e2e_s = max_over_ranks(e2e_s, world, dev)
+        # the link itself, for scale: one plain copy of the same pinned buffer to the device
+        scratch = torch.empty_like(edges)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        scratch.copy_(host, non_blocking=True)
+        ev1.record()
+        torch.cuda.synchronize()
+        link_gbs = 8 * E / (ev0.elapsed_time(ev1) / 1e3) / 1e9
+        del scratch
         e2e = {"value": round(world * E / e2e_s / 1e6, 3), "unit": "Medges/s", "h2d_bytes_per_step": 8 * E,
                "d2h_bytes_per_step": 4 * len(po) + 64, "ms_per_step": round(e2e_s * 1e3, 3),
                "per_step_ms": [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)],
-               "host_pinned": bool(host.is_pinned()),
+               "host_pinned": bool(host.is_pinned()), "h2d_copy_GBps": round(link_gbs, 1),
                "path": "eg_load_directed(host pinned records) + eg_get_partition"}
         # the same through the reference's input path: the binary edge file, streamed through
         # pinned staging buffers (eg_load_file); the file sits in the page cache after writing
