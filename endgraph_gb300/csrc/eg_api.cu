@@ -234,7 +234,12 @@ constexpr size_t kIngestPiece = 128ull << 20;
 class ReaderPool {
    public:
     ReaderPool(int fd, unsigned nt, const uint8_t* mem = nullptr) : fd_(fd), nt_(nt), mem_(mem) {
-        for (unsigned t = 0; t < nt; ++t) threads_.emplace_back([this, t] { run(t); });
+        try {
+            for (unsigned t = 0; t < nt; ++t) threads_.emplace_back([this, t] { run(t); });
+        } catch (...) {  // fewer threads than asked (none: the caller's thread reads)
+        }
+        std::lock_guard<std::mutex> lk(m_);
+        nt_ = (unsigned)threads_.size();
     }
     ~ReaderPool() {
         {
@@ -247,6 +252,7 @@ class ReaderPool {
     }
     // bytes [off, off + n) of the file into buf; false on a short read
     bool read(uint8_t* buf, uint64_t off, size_t n) {
+        if (nt_ == 0) return slice(buf, off, 0, n);
         {
             std::lock_guard<std::mutex> lk(m_);
             buf_ = buf;
@@ -280,25 +286,26 @@ class ReaderPool {
             }
             const size_t part = (n + nt_ - 1) / nt_;
             const size_t a = std::min(n, t * part), z = std::min(n, a + part);
-            size_t got = 0;
-            bool good = true;
-            if (mem_) {
-                memcpy(buf + a, mem_ + off + a, z - a);
-                got = z - a;
-            }
-            while (a + got < z) {
-                const ssize_t r = pread(fd_, buf + a + got, z - a - got, (off_t)(off + a + got));
-                if (r < 0 && errno == EINTR) continue;
-                if (r <= 0) {
-                    good = false;
-                    break;
-                }
-                got += (size_t)r;
-            }
+            const bool good = slice(buf, off, a, z);
             std::lock_guard<std::mutex> lk(m_);
             if (!good) ok_ = false;
             if (--pending_ == 0) done_.notify_one();
         }
+    }
+    // bytes [a, z) of the piece at off
+    bool slice(uint8_t* buf, uint64_t off, size_t a, size_t z) const {
+        if (mem_) {
+            memcpy(buf + a, mem_ + off + a, z - a);
+            return true;
+        }
+        size_t got = 0;
+        while (a + got < z) {
+            const ssize_t r = pread(fd_, buf + a + got, z - a - got, (off_t)(off + a + got));
+            if (r < 0 && errno == EINTR) continue;
+            if (r <= 0) return false;
+            got += (size_t)r;
+        }
+        return true;
     }
     int fd_;
     unsigned nt_;
@@ -388,7 +395,7 @@ int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V,
     up.issued = &issued;
     up.failed = &failed;
     cudaError_t stage_err = cudaSuccess;
-    std::thread stager([&]() {
+    auto stage = [&]() {
         cudaSetDevice(g->device);
         cudaEvent_t done[2] = {nullptr, nullptr};
         cudaError_t e = cudaSuccess;
@@ -417,9 +424,15 @@ int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V,
         cudaStreamSynchronize(g->copy_stream);  // the staging buffers are reused by the next call
         for (int i = 0; i < 2; ++i)
             if (done[i]) cudaEventDestroy(done[i]);
-    });
+    };
+    std::thread stager;
+    try {
+        stager = std::thread(stage);
+    } catch (...) {  // no thread to spare: upload everything first, then build
+        stage();
+    }
     const int st = build_structures(g, 1, 1, &up);
-    stager.join();
+    if (stager.joinable()) stager.join();
     if (st != EG_OK || stage_err != cudaSuccess) {
         g->V = 0;  // no usable edge list
         if (stage_err != cudaSuccess) return cuda_fail(stage_err, "eg_load_directed upload", __FILE__, __LINE__);
