@@ -223,6 +223,17 @@ __global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n
     if ((threadIdx.x & 31) == 0 && orr) atomicOr(alive_out, orr);
 }
 
+// zero the frontier words (and their renumbered copies) of the vertices a queue lists: the only
+// non-zero entries of a frontier array, cheaper than clearing all of it while frontiers are small
+__global__ void k_clear_front(const uint32_t* __restrict__ q, uint32_t n, unsigned long long* __restrict__ word,
+                              const uint32_t* __restrict__ new_id, unsigned long long* __restrict__ word_r) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = q[i];
+        word[v] = 0ull;
+        if (word_r) word_r[new_id[v]] = 0ull;
+    }
+}
+
 // the renumbered copy of the first frontier (the roots), which no level has listed
 __global__ void k_front_renumber(const uint32_t* __restrict__ q, const uint32_t* n_dev,
                                  const unsigned long long* __restrict__ word, const uint32_t* __restrict__ new_id,
@@ -749,6 +760,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
     const unsigned init_grid = std::max(1u, std::min<unsigned>((n_entries + 255) / 256, 4096u));
     const unsigned grid = (unsigned)g->num_sms * 8u;
     const bool one_graph = g->batch_voff.empty();
+    constexpr uint64_t kUnknownQueue = ~0ull;
     // pull gathers through the CSC sources renumbered by out-degree class (hot frontier words share
     // cache lines), with a renumbered copy of each frontier; on one graph with the host-driven loop
     const bool renum = one_graph && !g->use_cuda_graph && g->E > 0 && want_relabel(g);
@@ -788,17 +800,26 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
     // dense levels find most destinations nearly covered and use the early-exit pair -- on one
     // graph.  In a batch of graphs the running-root mask is shared by all graphs, so a vertex
     // waits for bits its own graph can never deliver, and every level keeps the chunked sweep.
+    // clear_n: how many vertices queue[x] lists from two levels back (the non-zero words of
+    // word[x]); kUnknownQueue when not known on the host, and the arrays are cleared whole
     auto enqueue_level = [&](uint32_t L, uint64_t n_host, bool dense, bool screen, uint32_t* count, const int* stop_flag,
-                             uint32_t* nout_host, unsigned long long* act_host, bool early_exit) -> int {
+                             uint32_t* nout_host, unsigned long long* act_host, bool early_exit, uint64_t clear_n) -> int {
         const int c = L & 1, x = c ^ 1;
-        EG_CUDA(cudaMemsetAsync(word[x], 0, 8 * V, g->stream));
+        if (clear_n <= V / 32) {
+            if (clear_n) {
+                Timed t(&g->prof, g->stream, "msbfs_vertex");
+                k_clear_front<<<grid_for(clear_n, 256, grid), 256, 0, g->stream>>>(
+                    queue[x], (uint32_t)clear_n, word[x], renum ? new_id : nullptr, renum ? word_r[x] : nullptr);
+                EG_CHECK_LAUNCH("k_clear_front");
+            }
+        } else {
+            EG_CUDA(cudaMemsetAsync(word[x], 0, 8 * V, g->stream));
+            if (renum) EG_CUDA(cudaMemsetAsync(word_r[x], 0, 8 * V, g->stream));
+        }
         EG_CUDA(cudaMemsetAsync(bm[x], 0, bm_bytes, g->stream));
         // renumbered gathers skip the frontier-bitmap screen (dense levels rarely screen)
         const unsigned long long* gather_word = renum ? word_r[c] : word[c];
-        if (renum) {
-            screen = false;
-            EG_CUDA(cudaMemsetAsync(word_r[x], 0, 8 * V, g->stream));
-        }
+        if (renum) screen = false;
         unsigned long long* alive_next = stop_flag ? nullptr : alive + x;
         if (alive_next) EG_CUDA(cudaMemsetAsync(alive_next, 0, 8, g->stream));
         if (dense) {
@@ -856,7 +877,8 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
                     k_level_gate<<<1, 1, 0, g->stream>>>(cnt + L - 1, stop);
                     st = cudaGetLastError() == cudaSuccess ? EG_OK : EG_ERR_CUDA;
                 }
-                if (st == EG_OK) st = enqueue_level(L, 0, true, true, cnt + L, stop, nullptr, nullptr, one_graph && L >= 3);
+                if (st == EG_OK)
+                    st = enqueue_level(L, 0, true, true, cnt + L, stop, nullptr, nullptr, one_graph && L >= 3, kUnknownQueue);
             }
             cudaGraph_t graph = nullptr;
             cudaError_t e = cudaStreamEndCapture(g->stream, &graph);
@@ -892,7 +914,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
                 set_error("eg_msbfs: more than 254 levels");
                 return EG_ERR_UNSUPPORTED;
             }
-            EG_TRY(enqueue_level(lvl, 0, true, true, d_new, stop, nullptr, nullptr, one_graph));
+            EG_TRY(enqueue_level(lvl, 0, true, true, d_new, stop, nullptr, nullptr, one_graph, kUnknownQueue));
             ++sweeps;
             uint32_t hn = 0;
             EG_CUDA(cudaMemcpyAsync(&hn, d_new, 4, cudaMemcpyDeviceToHost, g->stream));
@@ -912,6 +934,8 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         uint64_t n = h.n;
         unsigned long long act = h.act;
         int dense_levels = 0;
+        // host lengths of what queue[0] / queue[1] list; queue[1] still holds an earlier call's
+        uint64_t qlen[2] = {n, kUnknownQueue};
         while (n > 0) {
             if (lvl >= 254) {
                 set_error("eg_msbfs: more than 254 levels");
@@ -921,7 +945,8 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
             const bool dense = !g->built_csr || act >= g->E / (uint64_t)g->dense_div;
             uint32_t nout = 0;
             // a bitmap test before each gather pays only while the frontier is a small part of V
-            EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act, one_graph && dense_levels > 0));
+            EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act, one_graph && dense_levels > 0,
+                                 qlen[(lvl & 1) ^ 1]));
             if (dense) ++dense_levels;
             if (dense) {
                 EG_CUDA(cudaMemcpyAsync(&h, d_nq, 16, cudaMemcpyDeviceToHost, g->stream));
@@ -931,6 +956,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
             } else {
                 ++pushes;
             }
+            qlen[(lvl & 1) ^ 1] = nout;
             ++sweeps;
             n = nout;
             ++lvl;
