@@ -151,6 +151,33 @@ def test_pipelined_host_load_matches_device_load(eg_lib, weighted, pinned):
         assert np.array_equal(a.degrees()[1], b.degrees()[1])
 
 
+def test_pipelined_host_load_with_partitions(eg_lib):
+    """P = 4 takes the generic build: the pipelined upload waits for every part, validates, and
+    builds the same partitions and per-partition CSR / CSC as the device-resident load."""
+    import torch
+
+    import endgraph_gb300 as eg
+    V, E = 1 << 17, (1 << 22) + 77
+    src, dst, _ = rmat_graph(V, E, 321)
+    rec = eg.pack_edges(src, dst)
+    with eg.Graph(partitions=4) as a, eg.Graph(partitions=4) as b:
+        a.load_directed(rec, V)
+        b.load_edges(torch.from_numpy(rec.view(np.int32)).cuda(), V)
+        b.build()
+        pa, la = a.partition()
+        pb, lb = b.partition()
+        assert np.array_equal(pa, pb) and np.array_equal(la, lb)
+        ca, cb = a.csr(), b.csr()
+        ka, kb = a.csc(), b.csc()
+        for p in range(4):
+            assert lists_equal(ca["off"][p], ca["adj"], cb["off"][p], cb["adj"])
+            assert lists_equal(ka["off"][p], ka["adj"], kb["off"][p], kb["adj"])
+        bad = rec.copy()
+        bad[5, 0] = V + 3
+        with pytest.raises(eg.EndGraphError):
+            a.load_directed(bad, V)
+
+
 def test_more_partitions_than_pages(eg_lib):
     """P = 8 on a 5,000-vertex graph (two CPBT pages): most partitions are empty, as in the reference."""
     import endgraph_gb300 as eg
