@@ -372,13 +372,19 @@ int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V,
     cudaGetLastError();  // a pageable pointer may leave an error behind on older drivers
     free_batch_state(g);
     if (pinned) {  // the copy engines read the caller's buffer directly: every part queued now
-        for (int k = 0; k < K; ++k) {
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < K && e == cudaSuccess; ++k) {
             const size_t off = (size_t)up.e0[k] * edge_bytes, n = (size_t)(up.e0[k + 1] - up.e0[k]) * edge_bytes;
-            EG_CUDA(cudaMemcpyAsync(g->edges.as<uint8_t>() + off, src + off, n, cudaMemcpyHostToDevice, g->copy_stream));
-            EG_CUDA(cudaEventRecord(g->part_ready[k], g->copy_stream));
+            e = cudaMemcpyAsync(g->edges.as<uint8_t>() + off, src + off, n, cudaMemcpyHostToDevice, g->copy_stream);
+            if (e == cudaSuccess) e = cudaEventRecord(g->part_ready[k], g->copy_stream);
+        }
+        if (e != cudaSuccess) {  // copies already queued may still read the caller's buffer
+            cudaStreamSynchronize(g->copy_stream);
+            g->V = 0;
+            return cuda_fail(e, "cudaMemcpyAsync", __FILE__, __LINE__);
         }
         const int st = build_structures(g, 1, 1, &up);
-        const cudaError_t e = cudaStreamSynchronize(g->copy_stream);  // never return with the buffer in use
+        e = cudaStreamSynchronize(g->copy_stream);  // never return with the buffer in use
         if (st != EG_OK) {
             g->V = 0;  // no usable edge list
             return st;
