@@ -569,18 +569,24 @@ def run_ours(args, world, rank, local):
             with tempfile.TemporaryDirectory() as tmp:
                 path = os.path.join(tmp, "edges.bin")
                 h_np.tofile(path)
-                g2.load_file(path, V)
-                g2.build()
+                g2.load_directed_file(path, V)
                 g2.sync()
                 t0 = time.perf_counter()
+                for _ in range(n_e2e):
+                    g2.load_directed_file(path, V)
+                    po, _ = g2.partition()
+                g2.sync()
+                f_s = (time.perf_counter() - t0) / n_e2e
+                t0 = time.perf_counter()  # the two calls of the C++ header, which times the build alone
                 for _ in range(n_e2e):
                     g2.load_file(path, V)
                     g2.build()
                     po, _ = g2.partition()
                 g2.sync()
-                f_s = (time.perf_counter() - t0) / n_e2e
+                f2_s = (time.perf_counter() - t0) / n_e2e
             e2e["file"] = {"value": round(E / f_s / 1e6, 3), "unit": "Medges/s", "ms_per_step": round(f_s * 1e3, 3),
-                           "bytes_per_step": 8 * E, "path": "eg_load_file(binary edge file) + eg_build + eg_get_partition"}
+                           "bytes_per_step": 8 * E, "path": "eg_load_directed_file(binary edge file) + eg_get_partition",
+                           "load_then_build_ms": round(f2_s * 1e3, 3)}
         g2.close()
         del host
 

@@ -108,6 +108,7 @@ SIGNATURES = {
     "eg_profile_read": ([_vp, _vp, _i32, _vp], _i32),
     "eg_selftest_bounded_wait": ([_vp, _u32], _i32),
     "eg_load_file": ([_vp, ctypes.c_char_p, _u32, _i32, _i32], _i32),
+    "eg_load_directed_file": ([_vp, ctypes.c_char_p, _u32, _i32], _i32),
 }
 
 _lib = None
@@ -246,6 +247,11 @@ class Graph:
     def load_file(self, path, V, edge_bytes=8, symmetric=False):
         """Binary records {u32 src, u32 dst[, f32 w]} from a file (preload_graph_file)."""
         _check(self._L.eg_load_file(self.h, os.fsencode(path), V, edge_bytes, int(symmetric)))
+
+    def load_directed_file(self, path, V, edge_bytes=8):
+        """load_directed(path, V) in one call: the file is read and uploaded in parts while the
+        first build passes consume them."""
+        _check(self._L.eg_load_directed_file(self.h, os.fsencode(path), V, edge_bytes))
 
     def build(self, csr=True, csc=True):
         _check(self._L.eg_build(self.h, int(csr), int(csc)))

@@ -133,6 +133,12 @@ int eg_load_edges(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int ed
     return load_edges_impl(g, edges, E, V, edge_bytes, symmetric, where, true);
 }
 
+int eg_load_directed_file(eg_graph* g, const char* path, uint32_t V, int edge_bytes) {
+    EG_TRY(check_graph(g, "eg_load_directed_file"));
+    free_batch_state(g);
+    return eg::load_build_file(g, path, V, edge_bytes);
+}
+
 int eg_load_file(eg_graph* g, const char* path, uint32_t V, int edge_bytes, int symmetric) {
     EG_TRY(check_graph(g, "eg_load_file"));
     return load_file_impl(g, path, V, edge_bytes, symmetric);
@@ -340,7 +346,8 @@ static int ensure_staging(eg_graph* g) {
 // them: passes A and B of part k (and the id validation, in pass A) run on the handle's stream as
 // soon as part k has landed, so only the last part's passes and pass C follow the upload.  The
 // caller's buffer is read until this returns.
-int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes) {
+// mem: the records in host memory; else fd: a binary record file read by the staging thread
+static int pipelined_load(eg_graph* g, const uint8_t* mem, int fd, uint64_t E, uint32_t V, int edge_bytes) {
     EG_TRY(prepare_load(g, E, V, edge_bytes, 0));
     if (!g->copy_stream) EG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
     if (!g->copy_gate) EG_CUDA(cudaEventCreateWithFlags(&g->copy_gate, cudaEventDisableTiming));
@@ -365,10 +372,10 @@ int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V,
     // the records buffer may still be read by earlier work on the handle's stream
     EG_CUDA(cudaEventRecord(g->copy_gate, g->stream));
     EG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->copy_gate, 0));
-    const uint8_t* src = static_cast<const uint8_t*>(edges);
+    const uint8_t* src = mem;
     for (int k = 0; k < K; ++k) up.ready[k] = g->part_ready[k];
     cudaPointerAttributes attr{};
-    const bool pinned = cudaPointerGetAttributes(&attr, edges) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+    const bool pinned = mem && cudaPointerGetAttributes(&attr, mem) == cudaSuccess && attr.type == cudaMemoryTypeHost;
     cudaGetLastError();  // a pageable pointer may leave an error behind on older drivers
     free_batch_state(g);
     if (pinned) {  // the copy engines read the caller's buffer directly: every part queued now
@@ -392,23 +399,24 @@ int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V,
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
         return EG_OK;
     }
-    // pageable memory: a staging thread copies each part through the two pinned buffers (host
-    // threads memcpy a piece while the previous piece goes up) and records the part's event; the
-    // build waits for each event only after it has been recorded
+    // pageable memory or a file: a staging thread copies each part through the two pinned buffers
+    // (reader threads memcpy or pread a piece while the previous piece goes up) and records the
+    // part's event; the build waits for each event only after it has been recorded
     EG_TRY(ensure_staging(g));
     std::atomic<int> issued{0};
     std::atomic<bool> failed{false};
     up.issued = &issued;
     up.failed = &failed;
     cudaError_t stage_err = cudaSuccess;
+    uint64_t short_at = ~0ull;  // a short file read at this byte
     auto stage = [&]() {
         cudaSetDevice(g->device);
         cudaEvent_t done[2] = {nullptr, nullptr};
         cudaError_t e = cudaSuccess;
         for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
-        ReaderPool pool(-1, std::max(1u, std::min(16u, std::thread::hardware_concurrency())), src);
+        ReaderPool pool(fd, std::max(1u, std::min(16u, std::thread::hardware_concurrency())), src);
         uint64_t piece = 0;
-        for (int k = 0; k < K && e == cudaSuccess; ++k) {
+        for (int k = 0; k < K && e == cudaSuccess && short_at == ~0ull; ++k) {
             const uint64_t a = up.e0[k] * (uint64_t)edge_bytes, z = up.e0[k + 1] * (uint64_t)edge_bytes;
             for (uint64_t off = a; off < z && e == cudaSuccess; off += kIngestPiece, ++piece) {
                 const int slot = (int)(piece & 1);
@@ -416,14 +424,18 @@ int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V,
                 if (piece >= 2) e = cudaEventSynchronize(done[slot]);  // the copy that last used it
                 if (e != cudaSuccess) break;
                 const size_t n = (size_t)std::min<uint64_t>(kIngestPiece, z - off);
-                pool.read(buf, off, n);
+                if (!pool.read(buf, off, n)) {
+                    short_at = off;
+                    break;
+                }
                 e = cudaMemcpyAsync(g->edges.as<uint8_t>() + off, buf, n, cudaMemcpyHostToDevice, g->copy_stream);
                 if (e == cudaSuccess) e = cudaEventRecord(done[slot], g->copy_stream);
             }
+            if (short_at != ~0ull) break;
             if (e == cudaSuccess) e = cudaEventRecord(g->part_ready[k], g->copy_stream);
             if (e == cudaSuccess) issued.store(k + 1, std::memory_order_release);
         }
-        if (e != cudaSuccess) {
+        if (e != cudaSuccess || short_at != ~0ull) {
             stage_err = e;
             failed.store(true, std::memory_order_release);
         }
@@ -439,12 +451,52 @@ int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V,
     }
     const int st = build_structures(g, 1, 1, &up);
     if (stager.joinable()) stager.join();
-    if (st != EG_OK || stage_err != cudaSuccess) {
+    if (st != EG_OK || stage_err != cudaSuccess || short_at != ~0ull) {
         g->V = 0;  // no usable edge list
         if (stage_err != cudaSuccess) return cuda_fail(stage_err, "eg_load_directed upload", __FILE__, __LINE__);
+        if (short_at != ~0ull) {
+            set_error("eg_load_directed_file: short read in the piece at byte %llu", (unsigned long long)short_at);
+            return EG_ERR_INVALID;
+        }
         return st;
     }
     return EG_OK;
+}
+
+int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes) {
+    return pipelined_load(g, static_cast<const uint8_t*>(edges), -1, E, V, edge_bytes);
+}
+
+// binary records of a file, read and uploaded in parts while the build consumes them (directed)
+int load_build_file(eg_graph* g, const char* path, uint32_t V, int edge_bytes) {
+    if (!path) {
+        set_error("eg_load_directed_file: null path");
+        return EG_ERR_INVALID;
+    }
+    if (edge_bytes != 8 && edge_bytes != 12) {
+        set_error("eg_load_directed_file: edge_bytes must be 8 or 12");
+        return EG_ERR_INVALID;
+    }
+    const int fd = open(path, O_RDONLY);
+    if (fd < 0) {
+        set_error("eg_load_directed_file: cannot open %s", path);
+        return EG_ERR_INVALID;
+    }
+    struct stat st {};
+    if (fstat(fd, &st) != 0 || (uint64_t)st.st_size % (uint64_t)edge_bytes != 0) {
+        close(fd);
+        set_error("eg_load_directed_file: %s is not a whole number of %d-byte records", path, edge_bytes);
+        return EG_ERR_INVALID;
+    }
+    const uint64_t E = (uint64_t)st.st_size / (uint64_t)edge_bytes;
+    if (E < kPipelinedLoadMin) {  // small: read it, then build
+        close(fd);
+        EG_TRY(load_file_impl(g, path, V, edge_bytes, 0));
+        return build_structures(g, 1, 1);
+    }
+    const int r = pipelined_load(g, nullptr, fd, E, V, edge_bytes);
+    close(fd);
+    return r;
 }
 
 int load_file_impl(eg_graph* g, const char* path, uint32_t V, int edge_bytes, int symmetric) {

@@ -217,6 +217,7 @@ int build_structures(eg_graph* g, int want_csr, int want_csc, const UploadParts*
 // eg_load_directed of host records from this many records on: upload and build pipelined
 constexpr uint64_t kPipelinedLoadMin = 1ull << 22;
 int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes);
+int load_build_file(eg_graph* g, const char* path, uint32_t V, int edge_bytes);
 int compute_degrees(eg_graph* g);
 int cpbt_device(eg_graph* g, const uint32_t* d_deg, uint32_t V, int P, int S, uint64_t eta, int T, int dense,
                 uint32_t* h_part, uint32_t* h_local);

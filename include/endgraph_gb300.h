@@ -105,10 +105,13 @@ int eg_load_edges(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int ed
                   int where);
 
 /* The same from a binary edge file (the reference's input format, read whole as preload_graph_file
- * does for one rank, core/graph.hpp:1011-1084): 64 MiB pieces are read into pinned staging buffers
- * while the previous piece is copied to the device.  The file size must be a multiple of
+ * does for one rank, core/graph.hpp:1011-1084): 128 MiB pieces are read by a pool of reader threads
+ * into pinned staging buffers while the previous piece is copied to the device.  The file size must be a multiple of
  * edge_bytes. */
 int eg_load_file(eg_graph* g, const char* path, uint32_t V, int edge_bytes, int symmetric);
+/* load_directed(path, V) in one call: eg_load_file(..., 0) + eg_build(g, 1, 1), with the file read
+ * and uploaded in parts while the first build passes consume them (ids validated on the way). */
+int eg_load_directed_file(eg_graph* g, const char* path, uint32_t V, int edge_bytes);
 
 /* ---- preprocessing: split_graph core/graph.hpp:981-1009 ---------------------------------- */
 /* Degree histogram, CPBT partition (assign_vertices :662-792, dense out-degree weights with

@@ -215,9 +215,10 @@ def test_bounded_wait_runs_out_and_handle_survives(eg_lib):
 
 
 def test_file_ingest_matches_memory_load(eg_lib, tmp_path):
-    """eg_load_file (pieces read into pinned buffers while the previous piece is copied) loads the
-    same graph as eg_load_edges from memory; sizes that are not a multiple of the record size and
-    missing files are rejected."""
+    """eg_load_file (pieces read into pinned buffers while the previous piece is copied) and
+    eg_load_directed_file (read, uploaded and built in parts) load the same graph as the records
+    from memory; sizes that are not a multiple of the record size, missing files and ids >= V are
+    rejected."""
     import endgraph_gb300 as eg
     rng = np.random.default_rng(21)
     V, E = 50_000, 9_000_000  # 72 MB of 8-byte records: two staging pieces
@@ -228,13 +229,28 @@ def test_file_ingest_matches_memory_load(eg_lib, tmp_path):
         rec = eg.pack_edges(src, dst, w if weighted else None)
         f = tmp_path / f"g{int(weighted)}.bin"
         rec.tofile(f)
-        with eg.Graph() as a, eg.Graph() as b:
+        with eg.Graph() as a, eg.Graph() as b, eg.Graph() as c:
             a.load_file(str(f), V, rec.shape[1] * 4)
             a.build()
             b.load_directed(rec, V)
-            ca, cb = a.csr(), b.csr()
+            c.load_directed_file(str(f), V, rec.shape[1] * 4)  # 9 M records: four parts
+            ca, cb, cc = a.csr(), b.csr(), c.csr()
             assert lists_equal(ca["off"][0], ca["adj"], cb["off"][0], cb["adj"], ca["w"], cb["w"])
+            assert lists_equal(cc["off"][0], cc["adj"], cb["off"][0], cb["adj"], cc["w"], cb["w"])
+            ka, kc = a.csc(), c.csc()
+            assert lists_equal(kc["off"][0], kc["adj"], ka["off"][0], ka["adj"], kc["w"], ka["w"])
+            assert np.array_equal(kc["cvert"], ka["cvert"]) and np.array_equal(kc["cidx"], ka["cidx"])
             assert np.array_equal(a.partition()[0], b.partition()[0])
+            assert np.array_equal(c.partition()[0], b.partition()[0])
+    small = tmp_path / "small.bin"  # below the pipelined size: read, then built
+    eg.pack_edges(src[:1000], dst[:1000]).tofile(small)
+    with eg.Graph() as g:
+        g.load_directed_file(str(small), V)
+        assert g.info().E == 1000 and g.info().built_csr
+    oob = tmp_path / "oob.bin"
+    r = eg.pack_edges(src, dst)
+    r[E - 2, 1] = V
+    r.tofile(oob)
     bad = tmp_path / "bad.bin"
     bad.write_bytes(b"\0" * 20)
     with eg.Graph() as g:
@@ -242,3 +258,9 @@ def test_file_ingest_matches_memory_load(eg_lib, tmp_path):
             g.load_file(str(bad), 10, 8)
         with pytest.raises(eg.EndGraphError):
             g.load_file(str(tmp_path / "missing.bin"), 10, 8)
+        with pytest.raises(eg.EndGraphError):
+            g.load_directed_file(str(bad), 10, 8)
+        with pytest.raises(eg.EndGraphError):
+            g.load_directed_file(str(oob), V)
+        g.load_directed_file(str(small), V)  # the handle stays usable
+        assert g.info().E == 1000
