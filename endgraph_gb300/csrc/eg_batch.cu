@@ -29,7 +29,6 @@ namespace eg {
 
 constexpr uint32_t kTaskEdges = 512;
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
-constexpr int kRowWarps = 8;  // 256-thread blocks
 
 // ---------------------------------------------------------------------------------------------
 // MS-BFS.  A level is a pull sweep over the CSC when the frontier's out-edges reach E / divisor

@@ -146,7 +146,7 @@ static int push_level(eg_graph* g, const Op& op, uint32_t* q, uint64_t n, uint32
     return EG_OK;
 }
 
-static int copy_out(eg_graph* g, void* dst, const void* src, size_t bytes, int where) {
+static inline int copy_out(eg_graph* g, void* dst, const void* src, size_t bytes, int where) {
     if (!dst) return EG_OK;
     EG_CUDA(cudaMemcpyAsync(dst, src, bytes, where == EG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                             g->stream));
