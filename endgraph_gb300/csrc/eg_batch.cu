@@ -190,8 +190,9 @@ struct MsBfsPushOp {
     }
 };
 
-// level bytes of the queued vertices' new bits (row v of [V][64]: 16 threads, one 4-byte word
-// each) and the OR of their words, i.e. the roots whose traversal is still running
+// level bytes of the queued vertices' new bits (row v of [V][64]: 2 threads, two 16-byte quarters
+// each, a quarter rewritten only where one of its roots is new) and the OR of their words, i.e.
+// the roots whose traversal is still running
 // With new_id, the words are also copied to renumbered positions (next_r[new_id[v]]) for the pull
 // gathers that go through the renumbered CSC sources.
 __global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n_dev,
@@ -199,21 +200,32 @@ __global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n
                                unsigned long long* alive_out, const uint32_t* __restrict__ new_id,
                                unsigned long long* __restrict__ next_r) {
     const uint32_t n = __ldcg(n_dev);
-    const uint32_t sub = threadIdx.x & 15;
+    const uint32_t sub = threadIdx.x & 1u;
     const uint32_t fill = (lvl & 0xFFu) * 0x01010101u;
     unsigned long long orr = 0;
-    for (uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 4; i < n;
-         i += ((uint64_t)gridDim.x * blockDim.x) >> 4) {
+    for (uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 1; i < n;
+         i += ((uint64_t)gridDim.x * blockDim.x) >> 1) {
         const uint32_t v = q[i];
         const unsigned long long nb = next[v];
         if (new_id && sub == 0) next_r[new_id[v]] = nb;
         orr |= nb;
-        const uint32_t nib = (uint32_t)(nb >> (4 * sub)) & 0xFu;
-        if (levels && nib) {
-            // bit k of the nibble -> byte k all ones (the four shifted copies never overlap)
-            const uint32_t m = ((nib * 0x00204081u) & 0x01010101u) * 0xFFu;
-            uint32_t* p = reinterpret_cast<uint32_t*>(levels + (uint64_t)v * 64) + sub;
-            *p = (*p & ~m) | (fill & m);
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const uint32_t quarter = sub * 2 + c;
+            const uint32_t h = (uint32_t)(nb >> (16 * quarter)) & 0xFFFFu;
+            if (levels && h) {
+                uint4* p = reinterpret_cast<uint4*>(levels + (uint64_t)v * 64) + quarter;
+                uint4 x = *p;
+                uint32_t w[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    // bit j of the nibble -> byte j all ones (the shifted copies never overlap)
+                    const uint32_t nib = (h >> (4 * k)) & 0xFu;
+                    const uint32_t m = ((nib * 0x00204081u) & 0x01010101u) * 0xFFu;
+                    w[k] = (w[k] & ~m) | (fill & m);
+                }
+                *p = make_uint4(w[0], w[1], w[2], w[3]);
+            }
         }
     }
     if (!alive_out) return;
