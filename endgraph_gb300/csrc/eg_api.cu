@@ -374,15 +374,19 @@ static int pipelined_load(eg_graph* g, const uint8_t* mem, int fd, uint64_t E, u
     EG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->copy_gate, 0));
     const uint8_t* src = mem;
     for (int k = 0; k < K; ++k) up.ready[k] = g->part_ready[k];
+    // pinned host memory (or device / managed memory handed over as host: unified addressing
+    // copies it the same way) goes to the copy engines directly; pageable memory is staged
     cudaPointerAttributes attr{};
-    const bool pinned = mem && cudaPointerGetAttributes(&attr, mem) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+    const bool direct = mem && cudaPointerGetAttributes(&attr, mem) == cudaSuccess &&
+                        (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeDevice ||
+                         attr.type == cudaMemoryTypeManaged);
     cudaGetLastError();  // a pageable pointer may leave an error behind on older drivers
     free_batch_state(g);
-    if (pinned) {  // the copy engines read the caller's buffer directly: every part queued now
+    if (direct) {  // every part queued now
         cudaError_t e = cudaSuccess;
         for (int k = 0; k < K && e == cudaSuccess; ++k) {
             const size_t off = (size_t)up.e0[k] * edge_bytes, n = (size_t)(up.e0[k + 1] - up.e0[k]) * edge_bytes;
-            e = cudaMemcpyAsync(g->edges.as<uint8_t>() + off, src + off, n, cudaMemcpyHostToDevice, g->copy_stream);
+            e = cudaMemcpyAsync(g->edges.as<uint8_t>() + off, src + off, n, cudaMemcpyDefault, g->copy_stream);
             if (e == cudaSuccess) e = cudaEventRecord(g->part_ready[k], g->copy_stream);
         }
         if (e != cudaSuccess) {  // copies already queued may still read the caller's buffer

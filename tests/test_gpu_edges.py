@@ -149,6 +149,12 @@ def test_pipelined_host_load_matches_device_load(eg_lib, weighted, pinned):
             a.load_directed(bad, V)
         a.load_directed(rec, V)
         assert np.array_equal(a.degrees()[1], b.degrees()[1])
+        if not weighted and not pinned:  # device memory handed over as EG_HOST: copied as such
+            import ctypes
+            torch.cuda.synchronize()
+            st = eg_lib.eg_load_directed(a.h, ctypes.c_void_p(dev.data_ptr()), ctypes.c_uint64(E), V, 8, eg.EG_HOST)
+            assert st == 0, eg_lib.eg_last_error()
+            assert np.array_equal(a.degrees()[0], b.degrees()[0])
 
 
 def test_pipelined_host_load_with_partitions(eg_lib):
