@@ -150,45 +150,94 @@ def max_over_ranks(x, world, device=None):
 
 
 # ---------------------------------------------------------------------------------------------
-def reference_prep(V, E, seed, threads_note=True, steps=1, warmup=0):
-    """Time the reference's own preprocessing (oracle/_ref) on host cores; returns seconds list."""
+def workload_config(args, world):
+    """The `config` object of both arms' JSON lines (the same workload, the same keys)."""
+    V = 1 << args.scale
+    return {"workload": f"rmat-s{args.scale}-ef{args.edge_factor} CPBT+CSR+CSC, PageRank x{args.pr_iters}, "
+                        f"BFS x{args.roots} roots", "V": V, "E": V * args.edge_factor, "seed": args.seed,
+            "partitions": 1, "eta": 1, "l2": "inputs larger than L2 (4 GiB edge list, 2 GiB per structure)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def bench_root_edges(E, seed):
+    """Indices of 64 edges drawn by a seeded CPU generator: the bench's BFS roots are their
+    sources (non-isolated by construction), picked the same way by both arms."""
+    import torch
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    return torch.randint(0, E, (64,), generator=gen)
+
+
+def reference_workload(V, E, seed):
     import oracle
     if not oracle.Reference.available():
         if oracle.build_ref() is None:
             return None, "reference engine not built (reference sources absent on this machine)"
     src, dst, _ = oracle.rmat(V, E, seed, a=A, b=B, c=C, permute=True)
-    times = []
-    for i in range(warmup + steps):
-        R = oracle.Reference(src, dst, None, V, eta=1, max_iterations=20)
-        t = R.build()
-        R.close()
-        if i >= warmup:
-            times.append(t)
-    return times, int(oracle.Reference.lib().ref_threads())
+    return (src, dst), int(oracle.Reference.lib().ref_threads())
+
+
+def reference_analytics(R, src, dst, V, roots, pr_iters, pr_runs):
+    """The reference toolkits' exec_time on its own engine (oracle/_ref): PageRank (median of
+    pr_runs runs; the toolkit runs compute() four times, toolkits/pagerank.cpp:152-155) and BFS from
+    each root once (toolkits/bfs.cpp:114-138).  Returns a dict of times and GTEPS."""
+    import numpy as np
+
+    import oracle
+    pr_t = sorted(R.pagerank(pr_iters)[1] for _ in range(pr_runs))
+    t_pr = statistics.median(pr_t)
+    outd, _ = oracle.degrees(src, dst, V)
+    bfs_t, reach = [], 0
+    for r in roots:
+        lv, _, t = R.bfs(int(r))
+        bfs_t.append(t)
+        reach += int(outd[lv != oracle.UNREACHED].astype(np.uint64).sum())
+    return {"pagerank_s": round(t_pr, 4), "pagerank_runs": pr_runs,
+            "pagerank_gteps": round(pr_iters * len(src) / t_pr / 1e9, 3),
+            "bfs_s_per_root": round(sum(bfs_t) / len(bfs_t), 4), "bfs_roots": len(roots),
+            "bfs_gteps": round(reach / sum(bfs_t) / 1e9, 3)}
 
 
 def run_reference_arm(args, world, rank):
+    """The reference's own engine (oracle/_ref: core/graph.hpp compiled at one rank with every host
+    thread) on the same workload as our arm: each step is one split_graph of the full R-MAT
+    (prep_time, core/graph.hpp:1367-1371); PageRank and BFS exec times ride along."""
     if rank != 0:
         return
+    import oracle
     V = 1 << args.scale
     E = V * args.edge_factor
-    # bounded sample: the same generator at 1/8 of the edges and vertices (edge factor kept)
-    sv, se = V >> 3, E >> 3
-    times, threads = reference_prep(sv, se, args.seed, steps=args.steps, warmup=args.warmup)
-    if times is None:
+    wl, threads = reference_workload(V, E, args.seed)
+    if wl is None:
         print(json.dumps({"impl": "reference", "unavailable": threads}))
         return
+    src, dst = wl
+    times = []
+    R = None
+    for i in range(args.warmup + args.steps):
+        if R is not None:
+            R.close()
+        R = oracle.Reference(src, dst, None, V, eta=1, max_iterations=args.pr_iters)
+        t = R.build()
+        if i >= args.warmup:
+            times.append(t)
+    roots = [int(src[int(i)]) for i in bench_root_edges(E, args.seed)[:args.roots]]
+    ana = reference_analytics(R, src, dst, V, roots, args.pr_iters, 4)
+    R.close()
     t = sum(times) / len(times)
-    value = se / t / 1e6
+    value = E / t / 1e6
     line = {
         "impl": "reference", "metric": "preproc Medges/s", "value": round(value, 3), "unit": "Medges/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"rmat-s{args.scale}-ef{args.edge_factor} CPBT+CSR+CSC (load_directed)",
-                   "V": V, "E": E, "seed": args.seed},
+        "config": workload_config(args, 1),
+        "phases": {"prep_ms": round(t * 1e3, 3), "prep_medges_s": round(value, 1),
+                   "pagerank_ms": round(ana["pagerank_s"] * 1e3, 3), "pagerank_gteps": ana["pagerank_gteps"],
+                   "bfs_ms_per_root": round(ana["bfs_s_per_root"] * 1e3, 3), "bfs_gteps": ana["bfs_gteps"]},
         "cpu_baseline": {"value": round(value, 3), "unit": "Medges/s", "cores": threads, "kind": "reference",
-                         "sample": f"R-MAT V=2^{args.scale - 3}, E=2^{(E >> 3).bit_length() - 1} (same generator "
-                                   f"and edge factor, 1/8 of the workload), prep_time of split_graph per step"},
+                         "sample": f"the whole workload: split_graph (CPBT+CSR+CSC) of R-MAT V=2^{args.scale}, "
+                                   f"E={E} per step; PageRank x{args.pr_iters} exec_time median of 4 runs, "
+                                   f"BFS from the {len(roots)} bench roots once each",
+                         **ana},
         "e2e": {"value": round(value, 3), "unit": "Medges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -448,8 +497,7 @@ def run_ours(args, world, rank, local):
     edges = torch.empty((E, 2), dtype=torch.int32, device=dev)
     eg.generate_rmat(edges, V, E, seed, A, B, C, permute=True)
     torch.cuda.synchronize()
-    gen = torch.Generator(device="cpu").manual_seed(seed)
-    ridx = torch.randint(0, E, (64,), generator=gen)
+    ridx = bench_root_edges(E, seed)
     roots_all = [int(x) for x in edges[ridx.to(dev), 0].cpu().numpy().view(np.uint32)]
     roots = roots_all[:args.roots]
 
@@ -605,13 +653,18 @@ def run_ours(args, world, rank, local):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sv, se = V >> 3, E >> 3
-        times, threads = reference_prep(sv, se, args.seed, steps=1, warmup=0)
-        if times is not None:
-            cpu = {"value": round(se / times[0] / 1e6, 3), "unit": "Medges/s", "cores": threads,
-                   "kind": "reference",
-                   "sample": f"reference split_graph (CPBT+CSR+CSC) on R-MAT V=2^{args.scale - 3}, "
-                             f"E=2^{(se).bit_length() - 1} (same generator, edge factor {args.edge_factor})"}
+        import oracle
+        wl, threads = reference_workload(V, E, seed)
+        if wl is not None:
+            src, dst = wl
+            R = oracle.Reference(src, dst, None, V, eta=1, max_iterations=args.pr_iters)
+            t = R.build()
+            ana = reference_analytics(R, src, dst, V, roots, args.pr_iters, 1)
+            R.close()
+            cpu = {"value": round(E / t / 1e6, 3), "unit": "Medges/s", "cores": threads, "kind": "reference",
+                   "sample": f"the whole workload once: reference split_graph (CPBT+CSR+CSC) of the same R-MAT "
+                             f"(V=2^{args.scale}, E={E}), PageRank x{args.pr_iters} once, BFS from the "
+                             f"{len(roots)} bench roots once each", **ana}
         else:
             cpu = {"value": None, "unit": "Medges/s", "cores": 0, "kind": "reference", "sample": threads}
 
@@ -622,10 +675,7 @@ def run_ours(args, world, rank, local):
             "metric": "preproc Medges/s", "value": round(value, 3), "unit": "Medges/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": f"rmat-s{args.scale}-ef{args.edge_factor} CPBT+CSR+CSC, PageRank x{args.pr_iters}, "
-                                   f"BFS x{args.roots} roots", "V": V, "E": E, "seed": args.seed,
-                       "partitions": 1, "eta": 1, "l2": "inputs larger than L2 (4 GiB edge list, 2 GiB per structure)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": workload_config(args, world),
             "phases": {"prep_ms": round(t_prep, 3), "prep_medges_s": round(value / world, 1),
                        "prep_alg_GBps": round(prep_bytes / (t_prep / 1e3) / 1e9, 1),
                        "prep_frac_of_peak": round(prep_bytes / (t_prep / 1e3) / 1e9 / peak, 4),

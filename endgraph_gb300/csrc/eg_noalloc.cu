@@ -9,8 +9,12 @@
 // library holds until the process exits.
 //
 // The array is shared by all calls: calls on one device that overlap on the GPU (different streams,
-// different host threads) race on it and must be serialised by the caller.  Nothing in it has to
+// different host threads) race on it and must be serialised by the caller.  Its device address is
+// looked up on the first call on a device, and again on the first call after a device reset (a
+// new context); those calls should come before any stream capture.  Nothing in it has to
 // start at zero: every element a call reads was written earlier in the same call.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "eg_common.cuh"
@@ -51,9 +55,45 @@ __global__ void k_cpbt_to_vertices(const uint32_t* __restrict__ page_off, const 
     }
 }
 
-// device address of the scratch array, looked up once per device with that device current
+// Device address of the scratch array, looked up with the device current and kept per device
+// together with the unique id of the context it belongs to.  A context that is not the cached one
+// (after cudaDeviceReset the runtime makes a new primary context and loads the module again) gets
+// a fresh lookup, and the shared-memory attribute of k_cpbt is set again.  The context id comes
+// from the driver (cuCtxGetCurrent / cuCtxGetId, reached through the runtime's entry-point query,
+// so the library does not link libcuda); where it cannot be read, the first lookup per device is
+// kept.
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+struct NaDevice {
+    void* addr = nullptr;
+    unsigned long long ctx_id = 0;
+};
 static std::mutex g_na_mutex;
-static void* g_na_addr[128];
+static NaDevice g_na[128];
+
+static unsigned long long current_context_id() {
+    static bool queried = false;
+    static PfnCtxGetCurrent get_current = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    if (!queried) {
+        queried = true;
+        cudaDriverEntryPointQueryResult q;
+        void* f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PfnCtxGetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PfnCtxGetId>(f);
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS)
+        return id;
+    return 0;
+}
 
 static int noalloc_setup(int dev, unsigned char** out) {
     std::lock_guard<std::mutex> lock(g_na_mutex);
@@ -61,15 +101,18 @@ static int noalloc_setup(int dev, unsigned char** out) {
         set_error("eg_cpbt_partition_noalloc: device ordinal %d unsupported", dev);
         return EG_ERR_INVALID;
     }
-    if (!g_na_addr[dev]) {
+    NaDevice& d = g_na[dev];
+    const unsigned long long id = current_context_id();
+    if (!d.addr || (id != 0 && id != d.ctx_id)) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
         e = cudaFuncSetAttribute(k_cpbt, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_cpbt)", __FILE__, __LINE__);
-        g_na_addr[dev] = p;
+        d.addr = p;
+        d.ctx_id = id ? id : current_context_id();  // the lookup above made the context current
     }
-    *out = static_cast<unsigned char*>(g_na_addr[dev]);
+    *out = static_cast<unsigned char*>(d.addr);
     return EG_OK;
 }
 

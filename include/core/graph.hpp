@@ -70,18 +70,26 @@ class Graph {
     UINT owned_vertices = 0;
     UINT* degree = nullptr;                  // out-degree per vertex (host copy after load)
     UINT partition_offset_storage[2] = {0, 0};
-    UINT local_partition_offset_storage[2] = {0, 0};
+    std::vector<UINT> local_partition_offset_storage = std::vector<UINT>(2, 0);  // [sockets_num + 1]
     UINT* partition_offset = partition_offset_storage;
-    UINT* local_partition_offset = local_partition_offset_storage;
+    UINT* local_partition_offset = local_partition_offset_storage.data();
 
+    // The reference takes the rank count from MPI and the socket count from libnuma (init(),
+    // core/graph.hpp:202-285).  Here one process drives one GPU as one rank: EG_DEVICE picks the
+    // GPU (default 0) and EG_SUB_PARTITIONS the second-level CPBT split that sockets_num gives
+    // (default 1).  max_iterations is read at load time, as the reference reads it inside
+    // assign_vertices (:733-738).
     explicit Graph(int eta_) : eta((size_t)eta_) {
         eg_config cfg;
         cfg.eta = (uint64_t)eta_;
         cfg.partitions = 1;
-        cfg.sub_partitions = 1;
+        cfg.sub_partitions = env_int("EG_SUB_PARTITIONS", 1, 1, 64);
         cfg.max_iterations = 0;
-        cfg.device = 0;
+        cfg.device = env_int("EG_DEVICE", 0, 0, 1023);
         cfg.stream = nullptr;
+        sockets_num = cfg.sub_partitions;
+        local_partition_offset_storage.assign((size_t)sockets_num + 1, 0);
+        local_partition_offset = local_partition_offset_storage.data();
         eg_throw_if(eg_create(&handle_, &cfg), "eg_create");
     }
     ~Graph() {
@@ -114,25 +122,31 @@ class Graph {
         for (UINT v = 0; v < vertices_num; ++v) array[v] = value;
     }
     VertexSubset* alloc_vertex_subset() { return new VertexSubset(vertices_num); }
+    // One rank holds every vertex, so there is nothing to gather (core/graph.hpp:381-397 sends
+    // each rank's owned range to the root).
     template <typename T>
-    void gather_vertex_array(T*, int) {}  // one rank holds every vertex already
-    // raw sizeof(T) * V file, the reference's persistence format (core/graph.hpp:325-378)
+    void gather_vertex_array(T*, int) {}
+    // The reference's persistence format (core/graph.hpp:325-378): a raw file of sizeof(T) * V
+    // bytes.  dump creates it at that size when it is missing or has another size, then writes
+    // this rank's range [partition_offset[idx], partition_offset[idx + 1]) in place; restore
+    // refuses a file of another size and reads the same range.
     template <typename T>
     void dump_vertex_array(T* array, std::string path) {
-        FILE* f = fopen(path.c_str(), "wb");
-        if (!f) throw EndGraphError(EG_ERR_INVALID, "dump_vertex_array: cannot open " + path);
-        size_t n = fwrite(array, sizeof(T), vertices_num, f);
-        fclose(f);
-        if (n != vertices_num) throw EndGraphError(EG_ERR_INVALID, "dump_vertex_array: short write " + path);
+        const long file_length = (long)(sizeof(T) * (size_t)vertices_num);
+        if (!file_exists(path) || file_size(path) != file_length) {
+            int fd = open(path.c_str(), O_RDWR | O_CREAT | O_TRUNC, 0644);
+            if (fd < 0) throw EndGraphError(EG_ERR_INVALID, "dump_vertex_array: cannot create " + path);
+            const bool ok = ftruncate(fd, file_length) == 0;
+            close(fd);
+            if (!ok) throw EndGraphError(EG_ERR_INVALID, "dump_vertex_array: cannot size " + path);
+        }
+        io_range(array, path, true);
     }
     template <typename T>
     void restore_vertex_array(T* array, std::string path) {
-        if (file_size(path) != (long)(sizeof(T) * (size_t)vertices_num))
-            throw EndGraphError(EG_ERR_INVALID, "restore_vertex_array: size mismatch " + path);
-        FILE* f = fopen(path.c_str(), "rb");
-        size_t n = f ? fread(array, sizeof(T), vertices_num, f) : 0;
-        if (f) fclose(f);
-        if (n != vertices_num) throw EndGraphError(EG_ERR_INVALID, "restore_vertex_array: short read " + path);
+        if (!file_exists(path) || file_size(path) != (long)(sizeof(T) * (size_t)vertices_num))
+            throw EndGraphError(EG_ERR_INVALID, "restore_vertex_array: missing or size mismatch " + path);
+        io_range(array, path, false);
     }
 
     // ---- host-callback engine entry points: compile-compatible, refused at run time ----------
@@ -172,6 +186,38 @@ class Graph {
    private:
     eg_graph* handle_ = nullptr;
 
+    // pwrite / pread of this rank's range of a vertex array at its own offset in the file
+    template <typename T>
+    void io_range(T* array, const std::string& path, bool write_out) {
+        int fd = open(path.c_str(), O_RDWR);
+        if (fd < 0) throw EndGraphError(EG_ERR_INVALID, "vertex array file: cannot open " + path);
+        long offset = (long)(sizeof(T) * (size_t)partition_offset[partition_idx]);
+        const long end_offset = (long)(sizeof(T) * (size_t)partition_offset[partition_idx + 1]);
+        char* data = reinterpret_cast<char*>(array);
+        while (offset < end_offset) {
+            ssize_t n = write_out ? pwrite(fd, data + offset, end_offset - offset, offset)
+                                  : pread(fd, data + offset, end_offset - offset, offset);
+            if (n <= 0) {
+                close(fd);
+                throw EndGraphError(EG_ERR_INVALID, std::string("vertex array file: short ") +
+                                                        (write_out ? "write " : "read ") + path);
+            }
+            offset += n;
+        }
+        close(fd);
+    }
+
+    static int env_int(const char* name, int dflt, int lo, int hi) {
+        const char* v = getenv(name);
+        if (!v || !*v) return dflt;
+        char* end = nullptr;
+        long x = strtol(v, &end, 10);
+        if (*end || x < lo || x > hi)
+            throw EndGraphError(EG_ERR_INVALID, std::string(name) + ": expected an integer in [" + std::to_string(lo) +
+                                                    ", " + std::to_string(hi) + "], got '" + v + "'");
+        return (int)x;
+    }
+
     [[noreturn]] void refuse(const char* what) {
         throw EndGraphError(EG_ERR_HOST_CALLBACK,
                             std::string(what) +
@@ -181,6 +227,7 @@ class Graph {
 
     void load(const std::string& path, UINT vertices, bool symmetric) {
         const size_t rec = sizeof(EdgeType<EdgeData>);
+        eg_throw_if(eg_set_option(handle_, EG_OPT_MAX_ITERATIONS, max_iterations), "eg_set_option");
         eg_throw_if(eg_load_file(handle_, path.c_str(), vertices, (int)rec, symmetric ? 1 : 0), "eg_load_file");
         eg_info info;
         eg_throw_if(eg_get_info(handle_, &info), "eg_get_info");
@@ -195,7 +242,7 @@ class Graph {
         delete[] degree;
         degree = new UINT[vertices];
         eg_throw_if(eg_get_degrees(handle_, degree, nullptr, EG_HOST), "eg_get_degrees");
-        eg_throw_if(eg_get_partition(handle_, partition_offset_storage, local_partition_offset_storage),
+        eg_throw_if(eg_get_partition(handle_, partition_offset_storage, local_partition_offset_storage.data()),
                     "eg_get_partition");
     }
 };

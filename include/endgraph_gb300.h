@@ -150,8 +150,9 @@ int eg_optimal_offset(const uint64_t* a, uint32_t n, uint32_t k, uint32_t* offse
  * `stream` (a cudaStream_t; NULL is the legacy default stream).  It calls no cudaMalloc / cudaFree:
  * its scratch is a fixed array inside the library, EG_NOALLOC_SCRATCH_BYTES per GPU, kept until
  * process exit, which caps V, P and S at the limits below (larger requests return EG_ERR_INVALID).
- * The first call on a device looks up that array's device address; make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race and must be serialised. */
+ * The first call on a device looks up that array's device address (again after a device reset
+ * replaced the context); make that call before any stream capture.  Calls share the array: calls
+ * that overlap on the GPU race and must be serialised. */
 #define EG_NOALLOC_MAX_V (1u << 28)
 #define EG_NOALLOC_MAX_PARTITIONS 64
 #define EG_NOALLOC_MAX_SUB_PARTITIONS 16
@@ -189,11 +190,14 @@ enum {
     EG_OPT_SSSP_DELTA = 6,         /* eg_sssp near/far step in millionths of a weight unit; 0 = plain
                                       Bellman-Ford sweeps (the reference's order), -1 = automatic
                                       (0.7 x mean weight / mean out-degree; the default) */
-    EG_OPT_PR_RELABEL = 7          /* eg_pagerank gathers through a copy of the CSC source ids
+    EG_OPT_PR_RELABEL = 7,         /* eg_pagerank gathers through a copy of the CSC source ids
                                       renumbered by out-degree class, high degrees first, so that
                                       the values most gathered share cache lines; the same values
                                       are summed per destination.  1 on, 0 off, -1 automatic (on
                                       for V > 2^22; the default) */
+    EG_OPT_MAX_ITERATIONS = 8      /* T of the CPBT page weight for the next build (the public
+                                      max_iterations field of Graph, core/graph.hpp:733-738);
+                                      eg_config.max_iterations sets it at creation */
 };
 int eg_set_option(eg_graph* g, int option, int64_t value);
 

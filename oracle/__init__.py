@@ -50,6 +50,20 @@ def rmat_params(V, E, seed, a=0.57, b=0.19, c=0.19, permute=True, w_lo=0.0, w_hi
                       int((a + b + c) * 4294967296.0), 1 if permute else 0, w_lo, w_hi)
 
 
+def reference_dir() -> str | None:
+    """Directory of the reference checkout: $EG_REFERENCE_DIR, else the one build_ref.sh compiled
+    from (recorded in _ref/REFERENCE_DIR); None when neither exists on this machine."""
+    cand = [os.environ.get("EG_REFERENCE_DIR")]
+    rec = os.path.join(HERE, "_ref", "REFERENCE_DIR")
+    if os.path.exists(rec):
+        with open(rec) as f:
+            cand.append(f.read().strip())
+    for d in cand:
+        if d and os.path.isfile(os.path.join(d, "core", "graph.hpp")):
+            return d
+    return None
+
+
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "eg_oracle.c")
     if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < max(
@@ -98,6 +112,7 @@ def lib():
         L.ora_bc.argtypes = [_u64p, _u32p, ctypes.c_uint32, ctypes.c_uint32, _f64p, _f64p, _u32p]
         L.ora_adjacency_hash.argtypes = [_u32p, _u32p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                          _u64p, _u64p]
+        L.ora_list_hash.argtypes = [_u64p, _u32p, ctypes.c_void_p, ctypes.c_uint64, _u64p]
         _lib = L
     return _lib
 
@@ -223,6 +238,16 @@ def adjacency_hash(src, dst, w, V):
     return hout, hin
 
 
+def list_hash(off, adj, w=None):
+    """Per-list signature of a CSR/CSC (off[n+1], adj): equal to adjacency_hash's hout (CSR) or
+    hin (CSC) for the edge list it was built from, whatever the order inside each list."""
+    off = np.ascontiguousarray(off, np.uint64)
+    n = len(off) - 1
+    out = np.empty(max(n, 1), np.uint64)
+    lib().ora_list_hash(off, np.ascontiguousarray(adj, np.uint32), _ptr(w), n, out)
+    return out[:n]
+
+
 def sorted_lists(off, adj, w=None):
     """Per-list sort (by neighbour, then weight bits) for order-independent comparison."""
     off = np.asarray(off, np.int64)
@@ -265,6 +290,7 @@ class Reference:
             L.ref_num_compressed.argtypes = [vp]
             L.ref_num_compressed.restype = ctypes.c_uint64
             L.ref_get_structure.argtypes = [vp] * 13
+            L.ref_list_hashes.argtypes = [vp, vp, vp]
             L.ref_pagerank.argtypes = [vp, ctypes.c_int, vp]
             L.ref_pagerank.restype = ctypes.c_double
             L.ref_bfs.argtypes = [vp, ctypes.c_uint32, vp, vp]
@@ -313,6 +339,24 @@ class Reference:
         L.ref_get_structure(self.h, *[_ptr(d[k]) for k in (
             "degree", "partition_offset", "csr_src", "csr_dst", "csr_w", "csr_index", "csr_bitmap", "csc_src",
             "csc_dst", "csc_w", "cvert", "cidx")])
+        return d
+
+    def summary(self):
+        """The vertex-sized parts of the reference's structures (degrees, partition offsets, CSR
+        index and source bitmap, compressed CSC index) and per-vertex list signatures of its CSR
+        (hout) and CSC (hin): the whole structure without copying the edge-sized lists."""
+        L = self.lib()
+        V = self.V
+        nc = int(L.ref_num_compressed(self.h))
+        d = dict(degree=np.empty(V, np.uint32), partition_offset=np.empty(2, np.uint32),
+                 csr_index=np.empty(V + 1, np.uint64), csr_bitmap=np.empty(V // 64 + 1, np.uint64),
+                 cvert=np.empty(nc, np.uint32), cidx=np.empty(nc, np.uint64))
+        L.ref_get_structure(self.h, _ptr(d["degree"]), _ptr(d["partition_offset"]), None, None, None,
+                            _ptr(d["csr_index"]), _ptr(d["csr_bitmap"]), None, None, None, _ptr(d["cvert"]),
+                            _ptr(d["cidx"]))
+        d["hout"] = np.empty(V, np.uint64)
+        d["hin"] = np.empty(V, np.uint64)
+        L.ref_list_hashes(self.h, _ptr(d["hout"]), _ptr(d["hin"]))
         return d
 
     def pagerank(self, iterations=20):

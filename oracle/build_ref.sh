@@ -13,9 +13,11 @@
 #   -ffp-contract=off          IEEE double arithmetic identical on x86_64 and aarch64
 # `sparse` and `max_iterations` are given defined values by ref_driver.cpp before assign_vertices.
 #
-# Sources: $EG_REFERENCE_DIR (default /root/reference) when present.  A copy of the reference
-# headers is staged into oracle/_ref/src (git-ignored, never committed) so that the same build can
-# be repeated on a machine without the reference checkout.
+# Sources: $EG_REFERENCE_DIR, else the checkout at /root/reference, when present (this recipe is
+# the one place that names that location; oracle/_ref/REFERENCE_DIR records the directory it
+# used, and the tests that read reference files find it there).  A copy of the reference headers
+# is staged into oracle/_ref/src (git-ignored, never committed) so that the same build can be
+# repeated on a machine without the reference checkout.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
@@ -24,6 +26,7 @@ mkdir -p "$OUT/src/core"
 if [ -f "$REF/core/graph.hpp" ]; then
     cp "$REF"/core/*.hpp "$OUT/src/core/"
     INC="$REF"
+    (cd "$REF" && pwd) > "$OUT/REFERENCE_DIR"
 elif [ -f "$OUT/src/core/graph.hpp" ]; then
     INC="$OUT/src"
 else
@@ -31,7 +34,7 @@ else
     exit 3
 fi
 ${CXX:-g++} -O3 -std=c++14 -fopenmp -fno-strict-aliasing -ffp-contract=off -fPIC -shared -w \
-    -I"$HERE/ref" -I"$INC" \
+    -I"$HERE/ref" -I"$INC" -I"$HERE/../include" \
     -D'dense=(!sparse)' -Dout_degree=degree -Dedges=edges_num \
     -D'has_iterations=has_iterations; bool use_iteration = false; bool use_root = false' \
     "$HERE/ref/ref_driver.cpp" -o "$OUT/libeg_ref.so.tmp"

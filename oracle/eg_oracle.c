@@ -256,16 +256,25 @@ void ora_bfs_levels(const uint64_t* off, const uint32_t* adj, uint32_t V, uint32
 
 uint64_t ora_bfs_check_parents(const uint64_t* off, const uint32_t* adj, uint32_t V, uint32_t root,
                                const uint32_t* level, const uint32_t* parent) {
+    /* one pass over the edges marks every vertex whose parent holds an edge to it (O(V + E)) */
+    unsigned char* has_edge = (unsigned char*)calloc(V ? V : 1, 1);
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t u = 0; u < (int64_t)V; ++u)
+        for (uint64_t e = off[u]; e < off[u + 1]; ++e) {
+            const uint32_t v = adj[e];
+            if (v < V && parent[v] == (uint32_t)u) has_edge[v] = 1;
+        }
     uint64_t bad = 0;
-    for (uint32_t v = 0; v < V; ++v) {
+#pragma omp parallel for reduction(+ : bad) schedule(static)
+    for (int64_t i = 0; i < (int64_t)V; ++i) {
+        const uint32_t v = (uint32_t)i;
         if (level[v] == ORA_UNREACHED) { bad += parent[v] != V; continue; }
         if (v == root) { bad += parent[v] != root; continue; }
-        uint32_t u = parent[v];
+        const uint32_t u = parent[v];
         if (u >= V || level[u] == ORA_UNREACHED || level[u] + 1 != level[v]) { bad++; continue; }
-        int found = 0;
-        for (uint64_t e = off[u]; e < off[u + 1] && !found; ++e) found = adj[e] == v;
-        bad += !found;
+        bad += !has_edge[v];
     }
+    free(has_edge);
     return bad;
 }
 
@@ -376,5 +385,18 @@ void ora_adjacency_hash(const uint32_t* src, const uint32_t* dst, const float* w
         if (w) { uint32_t b; memcpy(&b, &w[i], 4); wb = (uint64_t)b << 32; }
         hout[src[i]] += eg_mix64(dst[i] | wb);
         hin[dst[i]] += eg_mix64(src[i] | wb);
+    }
+}
+
+void ora_list_hash(const uint64_t* off, const uint32_t* adj, const float* w, uint64_t n, uint64_t* h) {
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t v = 0; v < (int64_t)n; ++v) {
+        uint64_t acc = 0;
+        for (uint64_t e = off[v]; e < off[v + 1]; ++e) {
+            uint64_t wb = 0;
+            if (w) { uint32_t b; memcpy(&b, &w[e], 4); wb = (uint64_t)b << 32; }
+            acc += eg_mix64(adj[e] | wb);
+        }
+        h[v] = acc;
     }
 }

@@ -98,6 +98,11 @@ void ora_bc(const uint64_t* csr_off, const uint32_t* csr_dst, uint32_t V, uint32
 void ora_adjacency_hash(const uint32_t* src, const uint32_t* dst, const float* w, uint64_t E, uint32_t V,
                         uint64_t* hout, uint64_t* hin);
 
+/* The same signature per list of a CSR/CSC: h[v] = sum over [off[v], off[v+1]) of
+ * mix(adj[e] | wbits<<32), so h equals hout (CSR) or hin (CSC) of the edge list it was built from,
+ * whatever the order inside each list. */
+void ora_list_hash(const uint64_t* off, const uint32_t* adj, const float* w, uint64_t n, uint64_t* h);
+
 #ifdef __cplusplus
 }
 #endif

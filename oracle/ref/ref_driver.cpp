@@ -20,6 +20,7 @@
 #include <type_traits>
 
 #include "core/graph.hpp"
+#include "endgraph_rmat.h"  // eg_mix64, the signature mixing the oracle uses
 
 namespace {
 
@@ -59,12 +60,14 @@ Graph<E>* make_graph(const uint32_t* src, const uint32_t* dst, const float* w, u
     g->read_edges_num = n;
     size_t cap = (symmetric ? 2 : 1) * n;
     g->edge_list = (EdgeType<E>*)numa_alloc_interleaved(sizeof(EdgeType<E>) * (cap ? cap : 1));
+#pragma omp parallel for schedule(static)
     for (uint64_t i = 0; i < n; ++i) {
         g->edge_list[i].src = src[i];
         g->edge_list[i].dst = dst[i];
         if (!std::is_same<E, Empty>::value) memcpy((char*)&g->edge_list[i] + 8, &w[i], sizeof(float));
     }
     if (symmetric) {
+#pragma omp parallel for schedule(static)
         for (uint64_t i = 0; i < n; ++i) {
             g->edge_list[n + i].src = g->edge_list[i].dst;
             g->edge_list[n + i].dst = g->edge_list[i].src;
@@ -228,7 +231,7 @@ static void get_structure(Graph<E>* g, uint32_t* degree, uint32_t* partition_off
     size_t V = g->vertices_num;
     if (degree) memcpy(degree, g->degree, sizeof(uint32_t) * V);
     if (partition_offset) memcpy(partition_offset, g->partition_offset, sizeof(uint32_t) * 2);
-    for (uint64_t i = 0; i < g->outgoing_edges[0]; ++i) {
+    for (uint64_t i = 0; csr_src && i < g->outgoing_edges[0]; ++i) {
         EdgeType<E>& e = g->outgoing_adj_list[0][i];
         csr_src[i] = e.src;
         csr_dst[i] = e.dst;
@@ -236,19 +239,61 @@ static void get_structure(Graph<E>* g, uint32_t* degree, uint32_t* partition_off
     }
     if (csr_index) memcpy(csr_index, g->outgoing_adj_index[0], sizeof(uint64_t) * (V + 1));
     if (csr_bitmap) memcpy(csr_bitmap, g->outgoing_adj_bitmap[0]->data, sizeof(uint64_t) * (V / 64 + 1));
-    for (uint64_t i = 0; i < g->incoming_edges[0]; ++i) {
+    for (uint64_t i = 0; csc_src && i < g->incoming_edges[0]; ++i) {
         EdgeType<E>& e = g->incoming_adj_list[0][i];
         csc_src[i] = e.src;
         csc_dst[i] = e.dst;
         if (csc_w && !std::is_same<E, Empty>::value) memcpy(&csc_w[i], (char*)&e + 8, sizeof(float));
     }
-    for (uint32_t i = 0; i <= g->compressed_incoming_adj_vertices[0]; ++i) {
+    for (uint32_t i = 0; cvert && i <= g->compressed_incoming_adj_vertices[0]; ++i) {
         cvert[i] = g->compressed_incoming_adj_index[0][i].vertex;
         cidx[i] = g->compressed_incoming_adj_index[0][i].index;
     }
 }
 
+// Order-independent signature of every vertex's lists in the reference's own structures:
+// hout[v] = sum of mix(dst | wbits<<32) over v's outgoing list, hin[v] likewise over v's
+// incoming list (found through the compressed index).  Same mixing as the oracle's list hash.
+// outgoing_adj_index is written only at sources and one past them (core/graph.hpp:1329-1353), so
+// a list is read only where outgoing_adj_bitmap has the vertex.
+template <typename E>
+static void list_hashes(Graph<E>* g, uint64_t* hout, uint64_t* hin) {
+    const int64_t V = g->vertices_num;
+    const ULLONG* oi = g->outgoing_adj_index[0];
+    const EdgeType<E>* ol = g->outgoing_adj_list[0];
+    BitmapType* bm = g->outgoing_adj_bitmap[0];
+    auto wbits = [](const EdgeType<E>& e) -> uint64_t {
+        if (std::is_same<E, Empty>::value) return 0;
+        uint32_t b;
+        memcpy(&b, (const char*)&e + 8, 4);
+        return (uint64_t)b << 32;
+    };
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t v = 0; v < V; ++v) {
+        uint64_t acc = 0;
+        if (bm->get_bit((UINT)v))
+            for (ULLONG e = oi[v]; e < oi[v + 1]; ++e) acc += eg_mix64(ol[e].dst | wbits(ol[e]));
+        hout[v] = acc;
+        hin[v] = 0;
+    }
+    const int64_t nc = g->compressed_incoming_adj_vertices[0];
+    const CompressedAdjIndexType* ci = g->compressed_incoming_adj_index[0];
+    const EdgeType<E>* il = g->incoming_adj_list[0];
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t i = 0; i < nc; ++i) {
+        uint64_t acc = 0;
+        for (ULLONG e = ci[i].index; e < ci[i + 1].index; ++e) acc += eg_mix64(il[e].src | wbits(il[e]));
+        hin[ci[i].vertex] = acc;
+    }
+}
+
 extern "C" {
+
+void ref_list_hashes(void* hp, uint64_t* hout, uint64_t* hin) {
+    Handle* h = (Handle*)hp;
+    if (h->weighted) list_hashes((Graph<float>*)h->g, hout, hin);
+    else list_hashes((Graph<Empty>*)h->g, hout, hin);
+}
 
 /* number of compressed CSC entries including the sentinel (core/graph.hpp:1144-1188) */
 uint64_t ref_num_compressed(void* hp) {

@@ -105,8 +105,8 @@ def test_bfs_parent_checker_rejects_bad_trees(oracle_mod):
     assert oracle.bfs_check_parents(csr["off"][0], csr["adj"], V, r, lv, par) >= 1
 
 
-needs_ref = pytest.mark.skipif(not (oracle.Reference.available() or os.path.isdir("/root/reference")),
-                               reason="reference engine not built here")
+needs_ref = pytest.mark.skipif(not (oracle.Reference.available() or oracle.reference_dir()),
+                               reason="reference engine not built here (set EG_REFERENCE_DIR to build it)")
 
 
 @needs_ref
