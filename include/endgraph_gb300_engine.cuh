@@ -28,9 +28,22 @@
 //     __device__ R dense_slot(uint32_t dst, Acc acc) const;
 //   };
 //
-// Differences from the reference that an operator must respect: dense_slot sees the complete
-// reduction of a destination once (the reference may deliver one partial message per partition);
-// slots run concurrently and must use atomics for shared state, as the reference's slots do
+// With several CPBT partitions the engine runs Gemini's master/mirror message path
+// (core/graph.hpp:1445-1470, :1505-1802) over per-partition message buffers in device memory --
+// exactly what a multi-GPU build would exchange between ranks:
+//   sparse  every active master signals into the buffer of the partition that owns it
+//           ({vertex, msg} pairs, emit :1460); every partition then relaxes the messages of all
+//           buffers along its own CSR lists (the mirrors' slots, :1590-1655)
+//   dense   every partition reduces its in-edges (sources it owns) per destination and sends the
+//           partial to the destination's master partition as one {vertex, partial} message; each
+//           master buffer is then handed to dense_slot message by message (:1684-1801)
+// so dense_slot may see several partials of one destination, as in the reference; the slots of
+// the four toolkits combine them (write_add, cas, write_min).  With one partition, or with the
+// message path switched off, dense_slot sees the complete reduction of a destination once.
+// dense_selective (:1666-1682) is the subset the dense signals read; the reference sends each
+// rank's owned slice to every other rank first.  Here every partition reads the same device words,
+// so nothing moves; the slice volume is counted in message_stats() as what that exchange carries.
+// Slots run concurrently and must use atomics for shared state, as the reference's slots do
 // (core/atomic.hpp); a destination's contributions combine in any order.
 #pragma once
 
@@ -161,6 +174,110 @@ struct PullAdapter {
     }
 };
 
+// owner partition of v: last i with part_off[i] <= v (part_off: P+1 monotone offsets, v < part_off[P])
+__device__ __forceinline__ int owner_of(const uint32_t* __restrict__ part_off, int P, uint32_t v) {
+    int lo = 0, hi = P;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (part_off[mid] <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// message path, sparse signal: active masters emit into their own partition's buffer, which
+// starts at part_off[p] (a partition emits at most one message per vertex it owns)
+template <class Op>
+__global__ void k_signal_msgs(Op op, const uint32_t* __restrict__ q, const uint32_t* nq,
+                              const uint32_t* __restrict__ part_off, int P, uint32_t* __restrict__ mvert,
+                              typename Op::Msg* __restrict__ mdata, uint32_t* __restrict__ mcount) {
+    const uint32_t n = __ldcg(nq);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = q[i];
+        typename Op::Msg m;
+        if (op.sparse_signal(v, m)) {
+            const int p = owner_of(part_off, P, v);
+            const uint32_t at = part_off[p] + atomicAdd(mcount + p, 1u);
+            mvert[at] = v;
+            mdata[at] = m;
+        }
+    }
+}
+
+// message path, sparse receive: the buffers of all partitions, concatenated in partition order,
+// become the emitter queue of the slot pass and their payloads its per-vertex messages
+template <class Msg>
+__global__ void k_recv_msgs(const uint32_t* __restrict__ mvert, const Msg* __restrict__ mdata,
+                            const uint32_t* __restrict__ part_off, const uint32_t* __restrict__ mcount, int P,
+                            Msg* __restrict__ payload, uint32_t* __restrict__ q) {
+    uint32_t base = 0;
+    for (int p = 0; p < P; ++p) {
+        const uint32_t n = mcount[p];
+        for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+            const uint32_t at = part_off[p] + j;
+            const uint32_t v = mvert[at];
+            payload[v] = mdata[at];
+            q[base + j] = v;
+        }
+        base += n;
+    }
+}
+
+// message path, dense slots: every master partition's buffer, message by message
+template <class Op>
+__global__ void k_slot_msgs(Op op, const uint32_t* __restrict__ dvert, const typename Op::Acc* __restrict__ ddata,
+                            const uint64_t* __restrict__ dbase, const uint32_t* __restrict__ dcount, int P,
+                            typename Op::R* out) {
+    using R = typename Op::R;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (int i = 0; i < P; ++i) {
+        const uint64_t n = dcount[i], b = dbase[i];
+        for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+            const uint64_t j = base + threadIdx.x;
+            R r = R(0);
+            if (j < n) r = op.dense_slot(dvert[b + j], ddata[b + j]);
+            warp_add_out(r, out);
+        }
+    }
+}
+
+// message buffers per master partition of the dense path: entries with the destination's owner
+template <class Op>
+struct PullMsgAdapter {
+    using Acc = typename Op::Acc;
+    static constexpr bool kFilter = true;
+    Op op;
+    const float* w;
+    const uint32_t* part_off;
+    int P;
+    uint32_t* dvert;
+    Acc* ddata;
+    const uint64_t* dbase;  // [P+1] buffer starts; dbase[i+1] - dbase[i] = capacity of buffer i
+    uint32_t* dcount;
+    int* overflow;
+    __device__ bool stopped() const { return false; }
+    __device__ bool item_active(uint32_t v) const { return op.dense_active(v); }
+    __device__ Acc identity() const { return op.dense_identity(); }
+    __device__ Acc gather(uint32_t u, uint64_t pos) const { return op.dense_signal(u, w ? w[pos] : 0.f); }
+    __device__ Acc combine(Acc a, Acc b) const { return op.dense_combine(a, b); }
+    __device__ void smem_add(Acc* slot, Acc v) const {
+        if (to_bits(v) != to_bits(identity()))
+            atomic_combine(slot, v, [this](Acc x, Acc y) { return op.dense_combine(x, y); });
+    }
+    // one message per reduced piece of a (partition, destination) list; a list that crosses chunk
+    // boundaries sends one partial per chunk
+    __device__ void finish(bool ok, uint32_t v, Acc a, bool) const {
+        if (!ok || !op.dense_active(v) || to_bits(a) == to_bits(identity())) return;
+        const int i = owner_of(part_off, P, v);
+        const uint64_t at = dbase[i] + atomicAdd(dcount + i, 1u);
+        if (at < dbase[i + 1]) {
+            dvert[at] = v;
+            ddata[at] = a;
+        } else {
+            atomicExch(overflow, 1);
+        }
+    }
+};
+
 template <class Op>
 __global__ void k_sparse_signal(Op op, const uint32_t* __restrict__ q, const uint32_t* nq, typename Op::Msg* msg,
                                 uint32_t* q_out, uint32_t* n_out) {
@@ -227,6 +344,15 @@ __global__ void k_vertices(F f, const unsigned long long* __restrict__ words, ui
             }
         }
         warp_add_out(r, out);
+    }
+}
+
+// compressed items per owner partition of their destination (dense message buffer capacities)
+static __global__ void k_items_per_owner(const uint32_t* __restrict__ cvert, uint64_t nitems, uint32_t V,
+                                         const uint32_t* __restrict__ part_off, int P, unsigned long long* cnt) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nitems; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = cvert[i];
+        if (v < V) atomicAdd(cnt + owner_of(part_off, P, v), 1ull);
     }
 }
 
@@ -302,10 +428,21 @@ class Engine {
         f.nitems = info.ncompressed - 1;
         setup_pull_chunks(f);
         cur_ = &side_[0];
+        // CPBT partition offsets (the masters of each partition), host and device copies
+        h_part_off_.assign((size_t)P_ + 1, 0);
+        check_eg(eg_get_partition(g, h_part_off_.data(), nullptr), "eg_get_partition");
+        for (int i = 1; i <= P_; ++i) h_part_off_[i] = std::max(std::min(h_part_off_[i], V_), h_part_off_[i - 1]);
+        part_off_ = alloc<uint32_t>((size_t)P_ + 1);
+        check(cudaMemcpyAsync(part_off_, h_part_off_.data(), 4 * ((size_t)P_ + 1), cudaMemcpyHostToDevice, stream_),
+              "part_off");
+        check(cudaStreamSynchronize(stream_), "part_off");
+        msg_path_ = P_ > 1;
     }
     ~Engine() {
         for (void* p : {(void*)outdeg_, (void*)indeg_, (void*)counters_, (void*)q0_, (void*)q1_, (void*)ipref_,
-                        (void*)push_chunk_, (void*)scan_desc_, msg_, partial_, (void*)row_cvert_, (void*)row_cidx_})
+                        (void*)push_chunk_, (void*)scan_desc_, msg_, partial_, (void*)row_cvert_, (void*)row_cidx_,
+                        (void*)part_off_, (void*)mvert_, mdata_, (void*)mcount_, (void*)dvert_, ddata_, (void*)dbase_,
+                        (void*)dcount_})
             if (p) cudaFree(p);
         for (Side& sd : side_)
             for (void* p : {(void*)sd.chunk, (void*)sd.split})
@@ -333,6 +470,25 @@ class Engine {
     }
     bool transposed() const { return cur_ == &side_[1]; }
     uint64_t last_active_edges() const { return last_active_edges_; }
+
+    // The master/mirror message path over per-partition buffers (on by default with several
+    // partitions; off: the shared-memory engine, which needs no buffers and gives dense_slot the
+    // complete reduction of a destination).  As built only: the transposed graph has one partition.
+    void set_message_path(bool on) { msg_path_ = on && P_ > 1; }
+    bool message_path() const { return msg_path_; }
+    // what the last process_edges put in the partitions' buffers: messages per partition (sparse:
+    // by the master that emitted them; dense: by the master they are addressed to), and the bytes a
+    // rank-per-partition run would send: each sparse buffer to P-1 ranks, each dense message once
+    // (an upper bound: a partition's partials for its own masters stay local), and each rank's slice
+    // of dense_selective to P-1 ranks
+    struct MessageStats {
+        uint64_t messages = 0;
+        uint64_t bytes = 0;
+        uint64_t selective_bytes = 0;
+        std::vector<uint64_t> per_partition;
+    };
+    const MessageStats& message_stats() const { return stats_; }
+    const std::vector<uint32_t>& partition_offsets() const { return h_part_off_; }
 
     // vertex arrays and subsets in device memory (alloc_vertex_array / alloc_vertex_subset)
     template <class T>
@@ -388,10 +544,17 @@ class Engine {
     // core/graph.hpp:1473-1817.  Auto takes the sparse (push) path iff the active vertices' out-edges
     // are fewer than E / dense_divisor (the reference's E / 20, :1484-1491); the dense path does not
     // read `active` (an operator's dense_signal consults it, as the reference's dense_signal does).
+    // dense_selective: the subset the operator's dense signals read (the reference's
+    // process_edges argument); see the header comment for what happens to it.
     template <class Op>
-    typename Op::R process_edges(const Op& op, const Subset& active, Mode mode = Mode::Auto, int dense_divisor = 20) {
+    typename Op::R process_edges(const Op& op, const Subset& active, Mode mode = Mode::Auto, int dense_divisor = 20,
+                                 const Subset* dense_selective = nullptr) {
         using R = typename Op::R;
         static_assert(std::is_trivially_copyable<Op>::value, "operators are passed to kernels by value");
+        if (active.V != V_ || (dense_selective && dense_selective->V != V_))
+            throw Error(EG_ERR_INVALID, "process_edges: subsets must hold the graph's vertices");
+        stats_ = MessageStats();
+        stats_.per_partition.assign((size_t)P_, 0);
         R* out = reinterpret_cast<R*>(counters_ + 6);
         check(cudaMemsetAsync(out, 0, sizeof(R), stream_), "cudaMemsetAsync");
         uint32_t* d_n = reinterpret_cast<uint32_t*>(counters_ + 2);
@@ -414,8 +577,18 @@ class Engine {
             dense = mode == Mode::Auto && h.act >= E_ / (uint64_t)std::max(dense_divisor, 1);
         }
         last_dense_ = dense;
-        if (dense) run_dense(op, out);
-        else if (n_active) run_sparse(op, n_active, out);
+        if (dense && dense_selective && msg_path_) {
+            for (int i = 0; i < P_; ++i)
+                stats_.selective_bytes +=
+                    8ull * ((h_part_off_[i + 1] - h_part_off_[i]) / 64) * (uint64_t)(P_ - 1);
+        }
+        if (dense) {
+            if (msg_path_) run_dense_msgs(op, out);
+            else run_dense(op, out);
+        } else if (n_active) {
+            if (msg_path_) run_sparse_msgs(op, n_active, out);
+            else run_sparse(op, n_active, out);
+        }
         R h{};
         check(cudaMemcpyAsync(&h, out, sizeof(R), cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
         check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
@@ -423,6 +596,23 @@ class Engine {
     }
 
    private:
+    struct Side {
+        const uint64_t* push_off = nullptr;  // [P*(V+1)] list offsets of the push direction
+        const uint32_t* push_adj = nullptr;
+        const float* push_w = nullptr;
+        const uint32_t* push_deg = nullptr;  // list lengths (active-edge count of the switch)
+        const uint32_t* pull_adj = nullptr;
+        const float* pull_w = nullptr;
+        const uint32_t* pull_cvert = nullptr;  // compressed index of the pull direction
+        const uint64_t* pull_cidx = nullptr;
+        const uint32_t* pull_deg = nullptr;
+        uint64_t nitems = 0, nchunks = 0;
+        uint32_t* chunk = nullptr;  // first compressed entry per 4096-edge chunk
+        uint32_t* split = nullptr;  // entries whose list crosses a chunk boundary
+        unsigned long long nsplit = 0;
+        bool ready = false;
+    };
+
     template <class T>
     T* alloc(size_t n) {
         void* p = nullptr;
@@ -438,12 +628,7 @@ class Engine {
     template <class Op>
     void run_sparse(const Op& op, uint32_t n_active, typename Op::R* out) {
         using Msg = typename Op::Msg;
-        if (msg_bytes_ < sizeof(Msg) * (size_t)V_) {
-            if (msg_) cudaFree(msg_);
-            msg_ = nullptr;
-            check(cudaMalloc(&msg_, sizeof(Msg) * (size_t)V_), "cudaMalloc");
-            msg_bytes_ = sizeof(Msg) * (size_t)V_;
-        }
+        ensure_msg_arrays<Msg>();
         Msg* msg = static_cast<Msg*>(msg_);
         uint32_t* d_n = reinterpret_cast<uint32_t*>(counters_ + 2);
         uint32_t* d_emit = reinterpret_cast<uint32_t*>(counters_ + 4);
@@ -453,7 +638,60 @@ class Engine {
         uint32_t n_emit = 0;
         check(cudaMemcpyAsync(&n_emit, d_emit, 4, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
         check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        if (n_emit) push_emitters(op, msg, n_emit, out);
+    }
+
+    // master/mirror sparse step: masters signal into their partition's buffer; every partition
+    // relaxes all buffers along its own lists (the buffers, concatenated, are the emitter queue)
+    template <class Op>
+    void run_sparse_msgs(const Op& op, uint32_t n_active, typename Op::R* out) {
+        using Msg = typename Op::Msg;
+        ensure_msg_arrays<Msg>();
+        if (!mvert_) mvert_ = alloc<uint32_t>(V_);
+        if (mdata_bytes_ < sizeof(Msg) * (size_t)V_) {
+            if (mdata_) cudaFree(mdata_);
+            mdata_ = nullptr;
+            check(cudaMalloc(&mdata_, sizeof(Msg) * (size_t)V_), "cudaMalloc");
+            mdata_bytes_ = sizeof(Msg) * (size_t)V_;
+        }
+        if (!mcount_) mcount_ = alloc<uint32_t>((size_t)P_);
+        check(cudaMemsetAsync(mcount_, 0, 4 * (size_t)P_, stream_), "cudaMemsetAsync");
+        uint32_t* d_n = reinterpret_cast<uint32_t*>(counters_ + 2);
+        detail::k_signal_msgs<Op><<<grid(n_active), 256, 0, stream_>>>(op, q0_, d_n, part_off_, P_, mvert_,
+                                                                      static_cast<Msg*>(mdata_), mcount_);
+        check(cudaGetLastError(), "k_signal_msgs");
+        std::vector<uint32_t> cnt((size_t)P_);
+        check(cudaMemcpyAsync(cnt.data(), mcount_, 4 * (size_t)P_, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        uint64_t n_emit = 0;
+        for (int p = 0; p < P_; ++p) {
+            n_emit += cnt[p];
+            stats_.per_partition[p] = cnt[p];
+        }
+        stats_.messages = n_emit;
+        stats_.bytes = n_emit * (sizeof(uint32_t) + sizeof(Msg)) * (uint64_t)(P_ - 1);
         if (!n_emit) return;
+        Msg* payload = static_cast<Msg*>(msg_);
+        detail::k_recv_msgs<Msg><<<grid(n_emit), 256, 0, stream_>>>(mvert_, static_cast<const Msg*>(mdata_), part_off_,
+                                                                   mcount_, P_, payload, q1_);
+        check(cudaGetLastError(), "k_recv_msgs");
+        push_emitters(op, payload, (uint32_t)n_emit, out);
+    }
+
+    template <class Msg>
+    void ensure_msg_arrays() {
+        if (msg_bytes_ < sizeof(Msg) * (size_t)V_) {
+            if (msg_) cudaFree(msg_);
+            msg_ = nullptr;
+            check(cudaMalloc(&msg_, sizeof(Msg) * (size_t)V_), "cudaMalloc");
+            msg_bytes_ = sizeof(Msg) * (size_t)V_;
+        }
+    }
+
+    // relax the out-edges (every partition's list) of the n_emit emitters queued in q1_, whose
+    // messages are msg[v]
+    template <class Op>
+    void push_emitters(const Op& op, const typename Op::Msg* msg, uint32_t n_emit, typename Op::R* out) {
         // ranks of the emitters' out-edges (every partition's list of every emitter)
         const uint64_t nitems = (uint64_t)n_emit * P_;
         const uint64_t tiles = std::max<uint64_t>((nitems + kScanTile - 1) / kScanTile, 1);
@@ -530,22 +768,71 @@ class Engine {
         check(cudaGetLastError(), "k_dense_finish");
     }
 
-    struct Side {
-        const uint64_t* push_off = nullptr;  // [P*(V+1)] list offsets of the push direction
-        const uint32_t* push_adj = nullptr;
-        const float* push_w = nullptr;
-        const uint32_t* push_deg = nullptr;  // list lengths (active-edge count of the switch)
-        const uint32_t* pull_adj = nullptr;
-        const float* pull_w = nullptr;
-        const uint32_t* pull_cvert = nullptr;  // compressed index of the pull direction
-        const uint64_t* pull_cidx = nullptr;
-        const uint32_t* pull_deg = nullptr;
-        uint64_t nitems = 0, nchunks = 0;
-        uint32_t* chunk = nullptr;  // first compressed entry per 4096-edge chunk
-        uint32_t* split = nullptr;  // entries whose list crosses a chunk boundary
-        unsigned long long nsplit = 0;
-        bool ready = false;
-    };
+    // master/mirror dense step: each partition reduces its in-lists per destination (a list that
+    // crosses chunk boundaries gives one partial per chunk) and addresses the partial to the
+    // destination's master partition; each master buffer then goes through dense_slot
+    template <class Op>
+    void run_dense_msgs(const Op& op, typename Op::R* out) {
+        using Acc = typename Op::Acc;
+        const Side& sd = *cur_;
+        if (sd.nchunks == 0) return;
+        if (!dbase_) setup_dense_buffers(sd);
+        const uint64_t cap = h_dbase_[P_];
+        if (ddata_bytes_ < sizeof(Acc) * cap) {
+            if (ddata_) cudaFree(ddata_);
+            ddata_ = nullptr;
+            check(cudaMalloc(&ddata_, sizeof(Acc) * std::max<uint64_t>(cap, 1)), "cudaMalloc");
+            ddata_bytes_ = sizeof(Acc) * cap;
+        }
+        check(cudaMemsetAsync(dcount_, 0, 4 * ((size_t)P_ + 1), stream_), "cudaMemsetAsync");
+        int* overflow = reinterpret_cast<int*>(dcount_ + P_);
+        using K = detail::PullMsgAdapter<Op>;
+        K pa{op, sd.pull_w, part_off_, P_, dvert_, static_cast<Acc*>(ddata_), dbase_, dcount_, overflow};
+        const int cap_items = (int)kPullChunk + P_ + 2;
+        const size_t smem = pull_acc_offset(cap_items) + sizeof(Acc) * cap_items + cap_items;
+        check(cudaFuncSetAttribute(k_pull<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem");
+        int per_sm = 0;
+        check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<K>, kPullThreads, smem), "occupancy");
+        const unsigned g = (unsigned)std::min<uint64_t>(sd.nchunks, (uint64_t)num_sms_ * (uint64_t)std::max(per_sm, 1));
+        k_pull<K><<<g, kPullThreads, smem, stream_>>>(pa, sd.pull_adj, sd.pull_cidx, sd.pull_cvert, sd.chunk, E_,
+                                                     sd.nitems, sd.nchunks, V_, cap_items);
+        check(cudaGetLastError(), "k_pull");
+        detail::k_slot_msgs<Op><<<grid(cap), 256, 0, stream_>>>(op, dvert_, static_cast<const Acc*>(ddata_), dbase_,
+                                                               dcount_, P_, out);
+        check(cudaGetLastError(), "k_slot_msgs");
+        std::vector<uint32_t> cnt((size_t)P_ + 1);
+        check(cudaMemcpyAsync(cnt.data(), dcount_, 4 * ((size_t)P_ + 1), cudaMemcpyDeviceToHost, stream_),
+              "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        if (cnt[P_]) throw Error(EG_ERR_STATE, "process_edges: a dense message buffer overflowed");
+        for (int i = 0; i < P_; ++i) {
+            stats_.per_partition[i] = cnt[i];
+            stats_.messages += cnt[i];
+        }
+        stats_.bytes = stats_.messages * (sizeof(uint32_t) + sizeof(Acc));
+    }
+
+    // dense message buffers, one per master partition: capacity = the compressed entries whose
+    // destination it owns (one per (source partition, destination) list) + one per chunk boundary
+    void setup_dense_buffers(const Side& sd) {
+        unsigned long long* d_cnt = alloc<unsigned long long>((size_t)P_);
+        check(cudaMemsetAsync(d_cnt, 0, 8 * (size_t)P_, stream_), "cudaMemsetAsync");
+        detail::k_items_per_owner<<<grid(sd.nitems), 256, 0, stream_>>>(sd.pull_cvert, sd.nitems, V_, part_off_, P_,
+                                                                        d_cnt);
+        check(cudaGetLastError(), "k_items_per_owner");
+        std::vector<unsigned long long> cnt((size_t)P_);
+        check(cudaMemcpyAsync(cnt.data(), d_cnt, 8 * (size_t)P_, cudaMemcpyDeviceToHost, stream_), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        cudaFree(d_cnt);
+        h_dbase_.assign((size_t)P_ + 1, 0);
+        for (int i = 0; i < P_; ++i) h_dbase_[i + 1] = h_dbase_[i] + cnt[i] + sd.nchunks + 1;
+        dbase_ = alloc<uint64_t>((size_t)P_ + 1);
+        check(cudaMemcpyAsync(dbase_, h_dbase_.data(), 8 * ((size_t)P_ + 1), cudaMemcpyHostToDevice, stream_), "dbase");
+        dvert_ = alloc<uint32_t>(std::max<uint64_t>(h_dbase_[P_], 1));
+        dcount_ = alloc<uint32_t>((size_t)P_ + 1);
+        check(cudaStreamSynchronize(stream_), "dbase");
+    }
+
 
     void setup_pull_chunks(Side& sd) {
         sd.nchunks = (E_ + kPullChunk - 1) / kPullChunk;
@@ -637,6 +924,21 @@ class Engine {
     unsigned long long partial_id_ = 0;
     bool last_dense_ = false;
     uint64_t last_active_edges_ = 0;
+    // master/mirror message path
+    bool msg_path_ = false;
+    std::vector<uint32_t> h_part_off_;
+    uint32_t* part_off_ = nullptr;
+    uint32_t* mvert_ = nullptr;   // sparse buffers: partition p's messages start at part_off[p]
+    void* mdata_ = nullptr;
+    size_t mdata_bytes_ = 0;
+    uint32_t* mcount_ = nullptr;
+    uint32_t* dvert_ = nullptr;   // dense buffers: master partition i's messages start at dbase[i]
+    void* ddata_ = nullptr;
+    size_t ddata_bytes_ = 0;
+    uint64_t* dbase_ = nullptr;
+    std::vector<uint64_t> h_dbase_;
+    uint32_t* dcount_ = nullptr;  // [P] message counts, [P] overflow flag
+    MessageStats stats_;
 };
 
 }  // namespace engine

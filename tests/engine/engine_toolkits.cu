@@ -31,8 +31,10 @@ struct PrEdges {
     __device__ double dense_identity() const { return 0.0; }
     __device__ double dense_signal(uint32_t src, float) const { return curr[src]; }
     __device__ double dense_combine(double a, double b) const { return a + b; }
+    // write_add (toolkits/pagerank.cpp:91-94): with several partitions the partials of one
+    // destination arrive as separate messages
     __device__ int dense_slot(uint32_t dst, double sum) const {
-        next[dst] = sum;
+        atomicAdd(next + dst, sum);
         return 0;
     }
 };
@@ -65,36 +67,47 @@ struct Zero {
 };
 
 // ---- BFS, toolkits/bfs.cpp:22-112 ------------------------------------------------------------
+// visited is the dense_selective subset (bfs.cpp passes it to process_edges): the dense signals of
+// every partition skip visited destinations; the slots claim a parent with cas, so the first of
+// several partials wins
 struct BfsEdges {
     using Msg = uint32_t;
     using Acc = uint32_t;
     using R = unsigned int;
     uint32_t* parent;
-    uint32_t* level;
     uint32_t V;
-    uint32_t next_level;
-    Subset active_in, active_out;
+    Subset active_in, active_out, visited;
     __device__ bool sparse_signal(uint32_t v, uint32_t& msg) const {
         msg = v;
         return true;
     }
     __device__ unsigned sparse_slot(uint32_t, const uint32_t& src, uint32_t dst, float) const {
         if (__ldcg(parent + dst) == V && atomicCAS(parent + dst, V, src) == V) {
-            level[dst] = next_level;
             active_out.set_bit(dst);
             return 1u;
         }
         return 0u;
     }
-    __device__ bool dense_active(uint32_t dst) const { return __ldcg(parent + dst) == V; }
+    __device__ bool dense_active(uint32_t dst) const { return !visited.get_bit(dst); }
     __device__ uint32_t dense_identity() const { return 0xFFFFFFFFu; }
     __device__ uint32_t dense_signal(uint32_t src, float) const { return active_in.get_bit(src) ? src : 0xFFFFFFFFu; }
     __device__ uint32_t dense_combine(uint32_t a, uint32_t b) const { return a < b ? a : b; }
     __device__ unsigned dense_slot(uint32_t dst, uint32_t src) const {
         if (src == 0xFFFFFFFFu) return 0u;
-        parent[dst] = src;
-        level[dst] = next_level;
-        active_out.set_bit(dst);
+        if (atomicCAS(parent + dst, V, src) == V) {
+            active_out.set_bit(dst);
+            return 1u;
+        }
+        return 0u;
+    }
+};
+struct BfsVisit {  // bfs.cpp:77-84: mark the new frontier visited and record its level
+    Subset visited;
+    uint32_t* level;
+    uint32_t lvl;
+    __device__ unsigned operator()(uint32_t v) const {
+        visited.set_bit(v);
+        level[v] = lvl;
         return 1u;
     }
 };
@@ -188,6 +201,14 @@ static void write_out(FILE* f, const T* d, size_t n) {
     fwrite(h.data(), sizeof(T), n, f);
 }
 
+// messages the master/mirror path put in the partitions' buffers over the whole run
+static unsigned long long g_messages = 0, g_bytes = 0, g_selective = 0;
+static void tally(const Engine& g) {
+    g_messages += g.message_stats().messages;
+    g_bytes += g.message_stats().bytes;
+    g_selective += g.message_stats().selective_bytes;
+}
+
 int main(int argc, char** argv) {
     if (argc < 6) {
         fprintf(stderr, "usage: %s pagerank|bfs|cc|sssp <edge file> <V> <iterations|root> <out file>\n", argv[0]);
@@ -218,6 +239,7 @@ int main(int argc, char** argv) {
             for (uint32_t it = 0; it < arg; ++it) {
                 g.process_vertices<double>(Zero{next}, all);
                 g.process_edges(PrEdges{curr, next}, all, Mode::Dense);  // use_iteration: always dense
+                tally(g);
                 ++dense_steps;
                 g.process_vertices<double>(PrApply{next, g.out_degree(), 0.85, it == arg - 1}, all);
                 std::swap(curr, next);
@@ -231,14 +253,17 @@ int main(int argc, char** argv) {
             eg::engine::check(cudaMemcpy(parent + arg, &arg, 4, cudaMemcpyHostToDevice), "root");
             const uint32_t zero = 0;
             eg::engine::check(cudaMemcpy(level + arg, &zero, 4, cudaMemcpyHostToDevice), "root");
-            Subset a = g.alloc_subset(), b = g.alloc_subset();
+            Subset a = g.alloc_subset(), b = g.alloc_subset(), visited = g.alloc_subset();
             g.set_bit(a, arg);
+            g.set_bit(visited, arg);
             uint32_t active = 1;
             for (uint32_t lvl = 1; active > 0; ++lvl) {
                 g.clear(b);
                 // Gemini's switch: push while the frontier's out-edges stay below E/20
-                active = g.process_edges(BfsEdges{parent, level, V, lvl, a, b}, a, Mode::Auto);
+                g.process_edges(BfsEdges{parent, V, a, b, visited}, a, Mode::Auto, 20, &visited);
+                tally(g);
                 (g.last_was_dense() ? dense_steps : sparse_steps)++;
+                active = g.process_vertices<unsigned>(BfsVisit{visited, level, lvl}, b);
                 std::swap(a, b);
             }
             write_out(out, level, V);
@@ -254,6 +279,7 @@ int main(int argc, char** argv) {
             while (active > 0) {
                 g.clear(b);
                 active = g.process_edges(CcEdges{label, b}, a, Mode::Auto);
+                tally(g);
                 (g.last_was_dense() ? dense_steps : sparse_steps)++;
                 std::swap(a, b);
             }
@@ -269,6 +295,7 @@ int main(int argc, char** argv) {
             while (active > 0) {
                 g.clear(b);
                 active = g.process_edges(SsspEdges{dist, b}, a, Mode::Sparse);  // always sparse
+                tally(g);
                 ++sparse_steps;
                 std::swap(a, b);
             }
@@ -281,7 +308,9 @@ int main(int argc, char** argv) {
         }
     }
     fclose(out);
-    printf("{\"dense_steps\": %d, \"sparse_steps\": %d}\n", dense_steps, sparse_steps);
+    printf("{\"dense_steps\": %d, \"sparse_steps\": %d, \"messages\": %llu, \"message_bytes\": %llu, "
+           "\"selective_bytes\": %llu}\n",
+           dense_steps, sparse_steps, g_messages, g_bytes, g_selective);
     eg_destroy(h);
     return 0;
 }

@@ -1,5 +1,9 @@
 """The device operator API (include/endgraph_gb300_engine.cuh): the four reference toolkits written
-as signal/slot device functors (tests/engine/engine_toolkits.cu) against the oracle."""
+as signal/slot device functors (tests/engine/engine_toolkits.cu) against the oracle.  With several
+CPBT partitions every step goes through the master/mirror message path (per-partition buffers of
+{vertex, message} pairs, core/graph.hpp:1445-1470, :1505-1802); the run's JSON line reports the
+messages, so the tests check that they flowed."""
+import json
 import os
 import subprocess
 
@@ -36,6 +40,17 @@ def engine_exe(tmp_path_factory):
     return _compile(str(tmp_path_factory.mktemp("engine") / "engine_toolkits"))
 
 
+def _check_messages(log, P, selective=False):
+    st = json.loads(log.strip().splitlines()[-1])
+    if P > 1:
+        assert st["messages"] > 0 and st["message_bytes"] > 0, st
+        if selective:
+            assert st["selective_bytes"] > 0, st
+    else:
+        assert st["messages"] == 0, st
+    return st
+
+
 def _run(exe, tmp_path, algo, rec, V, arg, partitions=1):
     f = tmp_path / f"{algo}.bin"
     rec.tofile(f)
@@ -47,11 +62,13 @@ def _run(exe, tmp_path, algo, rec, V, arg, partitions=1):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("V,E,seed,P", [(1 << 14, 1 << 18, 5, 1), (100_000, 600_000, 6, 1), (100_000, 600_000, 6, 3)])
+@pytest.mark.parametrize("V,E,seed,P", [(1 << 14, 1 << 18, 5, 1), (100_000, 600_000, 6, 1), (100_000, 600_000, 6, 2),
+                                        (100_000, 600_000, 6, 4)])
 def test_engine_pagerank_fp64(engine_exe, tmp_path, V, E, seed, P):
     import endgraph_gb300 as eg
     src, dst, _ = rmat_graph(V, E, seed)
-    out, _ = _run(engine_exe, tmp_path, "pagerank", eg.pack_edges(src, dst), V, 20, P)
+    out, log = _run(engine_exe, tmp_path, "pagerank", eg.pack_edges(src, dst), V, 20, P)
+    _check_messages(log, P)
     pr = np.fromfile(out, np.float64)
     o_out, _ = oracle.degrees(src, dst, V)
     csc = oracle.build_csc(src, dst, None, V, np.array([0, V], np.uint32))
@@ -60,7 +77,8 @@ def test_engine_pagerank_fp64(engine_exe, tmp_path, V, E, seed, P):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("V,E,seed,P", [(1 << 14, 1 << 18, 7, 1), (1 << 16, 1 << 20, 8, 1), (1 << 16, 1 << 20, 8, 2)])
+@pytest.mark.parametrize("V,E,seed,P", [(1 << 14, 1 << 18, 7, 1), (1 << 16, 1 << 20, 8, 1), (1 << 16, 1 << 20, 8, 2),
+                                        (1 << 16, 1 << 20, 8, 4)])
 def test_engine_bfs(engine_exe, tmp_path, V, E, seed, P):
     import endgraph_gb300 as eg
     src, dst, _ = rmat_graph(V, E, seed)
@@ -72,24 +90,29 @@ def test_engine_bfs(engine_exe, tmp_path, V, E, seed, P):
     assert np.array_equal(lv, oracle.bfs_levels(csr["off"][0], csr["adj"], V, root))
     assert oracle.bfs_check_parents(csr["off"][0], csr["adj"], V, root, lv, par) == 0
     assert '"dense_steps": 0' not in log  # the E/20 switch took the pull path at least once
+    _check_messages(log, P, selective=True)  # visited is the dense_selective subset
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("V,E,seed,P", [(1 << 14, 1 << 17, 9, 1), (100_000, 300_000, 10, 1), (100_000, 300_000, 10, 4)])
+@pytest.mark.parametrize("V,E,seed,P", [(1 << 14, 1 << 17, 9, 1), (100_000, 300_000, 10, 1), (100_000, 300_000, 10, 2),
+                                        (100_000, 300_000, 10, 4)])
 def test_engine_cc(engine_exe, tmp_path, V, E, seed, P):
     import endgraph_gb300 as eg
     src, dst, _ = rmat_graph(V, E, seed)
-    out, _ = _run(engine_exe, tmp_path, "cc", eg.pack_edges(src, dst), V, 0, P)
+    out, log = _run(engine_exe, tmp_path, "cc", eg.pack_edges(src, dst), V, 0, P)
+    _check_messages(log, P)
     assert np.array_equal(np.fromfile(out, np.uint32), oracle.cc_labels(src, dst, V))
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("V,E,seed", [(1 << 14, 1 << 17, 11), (50_000, 400_000, 12)])
-def test_engine_sssp(engine_exe, tmp_path, V, E, seed):
+@pytest.mark.parametrize("V,E,seed,P", [(1 << 14, 1 << 17, 11, 1), (50_000, 400_000, 12, 1), (50_000, 400_000, 12, 2),
+                                        (50_000, 400_000, 12, 4)])
+def test_engine_sssp(engine_exe, tmp_path, V, E, seed, P):
     import endgraph_gb300 as eg
     src, dst, w = rmat_graph(V, E, seed, weights=(0.0, 1.0))
     root = int(src[0])
-    out, _ = _run(engine_exe, tmp_path, "sssp", eg.pack_edges(src, dst, w), V, root)
+    out, log = _run(engine_exe, tmp_path, "sssp", eg.pack_edges(src, dst, w), V, root, P)
+    _check_messages(log, P)
     d = np.fromfile(out, np.float32)
     csr = oracle.build_csr(src, dst, w, V, np.array([0, V], np.uint32))
     ref = oracle.sssp(csr["off"][0], csr["adj"], csr["w"], V, root)
