@@ -347,11 +347,48 @@ def run_batched(args, g, edges, roots, dev, stream):
         dw = torch.empty_like(w)
         gp.ppr_backward(w, seeds, dl, 0.15, K, dl_dw=dw)
         t_bw, _ = _timed(s2, lambda: gp.ppr_backward(w, seeds, dl, 0.15, K, dl_dw=dw))
+        # algorithmic bytes: a forward step reads the CSC ids and normalised weights (8E) and one
+        # 64-column row (256 B) per vertex, and writes one; an adjoint step reads the CSR ids and
+        # weights (8E), reads and writes the per-edge gradient accumulator (8E), and reads lambda and
+        # x_k rows and writes lambda rows (3 x 256 B per vertex); the adjoint also runs the forward
+        # twice (the checkpointed pass, then the iterates between checkpoints)
+        fwd_step = 8 * Ep + 2 * 256 * Vp
+        adj_step = 16 * Ep + 3 * 256 * Vp
+        peak, _ = measured_peaks()
+        fwd_gbs = K * fwd_step / (t_b / 1e3) / 1e9
+        adj_gbs = (K * adj_step + 2 * K * fwd_step) / (t_bw / 1e3) / 1e9
         res["ppr64"] = {"V": Vp, "E": Ep, "seeds": 64, "iterations": K, "alpha": 0.15,
                         "plain_ms": round(t_plain, 3), "batched_ms": round(t_b, 3),
                         "plain_gteps": round(64 * K * Ep / t_plain / 1e6, 2),
                         "batched_gteps": round(64 * K * Ep / t_b / 1e6, 2), "speedup": round(t_plain / t_b, 2),
-                        "adjoint_ms": round(t_bw, 3)}
+                        "adjoint_ms": round(t_bw, 3), "forward_alg_GBps": round(fwd_gbs, 1),
+                        "forward_frac_of_peak": round(fwd_gbs / peak, 4), "adjoint_alg_GBps": round(adj_gbs, 1),
+                        "adjoint_frac_of_peak": round(adj_gbs / peak, 4)}
+    del ep, w
+    torch.cuda.empty_cache()
+    # batched SSSP (64 sources, one row of 64 distances per vertex) against 64 single-source runs
+    # on the same weighted R-MAT (2^ppr_scale vertices, edge factor 16, U[0,1) weights)
+    rec = torch.empty((Ep, 3), dtype=torch.int32, device=dev)
+    eg.generate_rmat(rec, Vp, Ep, args.seed + 9, 0.57, 0.19, 0.19, permute=True, weights=(0.0, 1.0))
+    srcs = rec[:64, 0].cpu().numpy().view(np.uint32).copy()
+    with eg.Graph(eta=1, device=dev.index or 0) as gs:
+        gs.load_directed(rec, Vp)
+        del rec
+        s3 = torch.cuda.ExternalStream(gs.stream, device=dev)
+        d1 = torch.empty(Vp, dtype=torch.float32, device=dev)
+        d64 = torch.empty((64, Vp), dtype=torch.float32, device=dev)
+        gs.sssp(int(srcs[0]), d1)
+
+        def plain_sssp():
+            for r in srcs:
+                gs.sssp(int(r), d1)
+
+        t_plain, _ = _timed(s3, plain_sssp)
+        gs.sssp_batch(srcs, d64)
+        t_b, _ = _timed(s3, lambda: gs.sssp_batch(srcs, d64))
+        res["sssp64"] = {"V": Vp, "E": Ep, "sources": 64, "plain_ms": round(t_plain, 3), "batched_ms": round(t_b, 3),
+                         "speedup": round(t_plain / t_b, 2), "sweeps": gs.last_run()["iterations"]}
+    torch.cuda.empty_cache()
     return res
 
 
@@ -585,7 +622,7 @@ def run_ours(args, world, rank, local):
         g2 = eg.Graph(eta=1, partitions=1, max_iterations=args.pr_iters, device=local)
         g2.load_directed(h_np, V)
         g2.sync()
-        n_e2e = max(2, min(args.steps, 5))
+        n_e2e = max(3, min(args.steps, 9))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         marks = []
@@ -594,8 +631,11 @@ def run_ours(args, world, rank, local):
             po, _ = g2.partition()
             marks.append(time.perf_counter())
         g2.sync()
-        e2e_s = (time.perf_counter() - t0) / n_e2e
-        e2e_s = max_over_ranks(e2e_s, world, dev)
+        per_step = [b - a for a, b in zip([t0] + marks[:-1], marks)]
+        # the median step: one stalled step of the host (page faults, another tenant's process)
+        # would otherwise set the figure; the mean is reported beside it
+        e2e_mean = (time.perf_counter() - t0) / n_e2e
+        e2e_s = max_over_ranks(statistics.median(per_step), world, dev)
         # the link itself, for scale: one plain copy of the same pinned buffer to the device
         scratch = torch.empty_like(edges)
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -607,7 +647,8 @@ def run_ours(args, world, rank, local):
         del scratch
         e2e = {"value": round(world * E / e2e_s / 1e6, 3), "unit": "Medges/s", "h2d_bytes_per_step": 8 * E,
                "d2h_bytes_per_step": 4 * len(po) + 64, "ms_per_step": round(e2e_s * 1e3, 3),
-               "per_step_ms": [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)],
+               "ms_per_step_mean": round(e2e_mean * 1e3, 3), "statistic": "median step",
+               "per_step_ms": [round(x * 1e3, 2) for x in per_step],
                "host_pinned": bool(host.is_pinned()), "h2d_copy_GBps": round(link_gbs, 1),
                "path": "eg_load_directed(host pinned records) + eg_get_partition"}
         # the same through the reference's input path: the binary edge file, streamed through
