@@ -421,15 +421,21 @@ def run_graph_batch(args, dev):
         torch.cuda.empty_cache()
         out["build_ms"] = round(t_b, 3)
         out["build_medges_s"] = round(E / t_b / 1e3, 1)
-        tune = g.autotune(roots[:64])  # graph 0's roots are union ids too (its offset is 0)
+        # tune on one root from each of 64 graphs spread over the size range (union ids)
+        voff, _ = g.graph_batch()
+        pick = np.linspace(0, G - 1, 64).astype(np.int64)
+        tune = g.autotune((roots[pick * 64] + voff[pick]).astype(np.uint32))
         out["autotune"] = tune
         lev = torch.empty((int(Vs.sum()), 64), dtype=torch.uint8, device=dev)
         for cg in (0, 1):
             g.set_option(eg.EG_OPT_CUDA_GRAPH, cg)
             g.msbfs_graphs(roots, 64, lev)
             t, (_, edges) = _timed(s, lambda: g.msbfs_graphs(roots, 64, lev))
-            out[f"msbfs_{'graph' if cg else 'host'}_ms"] = round(t, 3)
-            out[f"msbfs_{'graph' if cg else 'host'}_gteps"] = round(edges / t / 1e6, 1)
+            mode = "graph" if cg else "host"
+            run = g.last_run()
+            out[f"msbfs_{mode}_ms"] = round(t, 3)
+            out[f"msbfs_{mode}_gteps"] = round(edges / t / 1e6, 1)
+            out[f"msbfs_{mode}_levels"] = [run["push"], run["pull"]]
         g.set_option(eg.EG_OPT_CUDA_GRAPH, tune["cuda_graph"])
         del lev
         dist = torch.empty((int(Vs.sum()), 64), dtype=torch.float32, device=dev)

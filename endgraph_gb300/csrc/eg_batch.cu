@@ -659,6 +659,7 @@ int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E) {
 struct BatchState {
     DevBuf a64, b64, c64, lev, rows0, rows1, heavy, tmp_out, seeds, wn_csc, wn_csr, s_out, gA, row_of, ck, seg;
     DevBuf ch0, ch1, flag, level_cnt, entries, n_entries, bm0, bm1, alive, ms_seg;
+    DevBuf cap;  // captured level loop: per-level direction decisions and frontier edge counts
     DevBuf wr0, wr1;  // frontier words in renumbered order (pull gathers through renumbered sources)
     RowTasks csc_tasks, csr_tasks;
     bool csc_ready = false, csr_ready = false;
@@ -739,12 +740,58 @@ __global__ void k_msbfs_init_entries(const uint2* ent, const uint32_t* n_dev, un
     }
 }
 
-// in a captured level loop: level L runs only if level L-1 found something
-__global__ void k_level_gate(const uint32_t* prev_new, int* stop) {
-    if (*prev_new == 0) *stop = 1;
+constexpr int kGraphLevels = 16;
+
+// The captured level loop makes, on the device, the choice the host loop makes per level: each
+// level's first kernel reads the frontier's length and out-edges and arms either the pull kernels
+// (the chunked sweep for the first dense level, the early-exit pair after it on one graph) or the
+// push (a scan and expansion whose item count it sets); the kernels of the other path find
+// nothing to do.  After an empty frontier every later level is disarmed.
+struct CapLevel {
+    uint32_t n_push;   // queue length handed to the push scan and expansion (0: pull level)
+    int skip_direct;   // k_pull_direct (MsBfsPullOp::stop)
+    int skip_early;    // k_ms_head / k_ms_tail (MsBuArgs::stop)
+    int pad;
+};
+struct CapState {
+    CapLevel lv[kGraphLevels];
+    unsigned long long act[kGraphLevels];  // out-edges of the frontier level L produced
+    uint64_t push_total;                   // edges of the current push level (scan total)
+    int dense_count;
+    int stop;
+};
+
+__global__ void k_cap_decide(CapState* st, int L, const uint32_t* n_src, const unsigned long long* act_src,
+                             unsigned long long dense_min, int early_after_first, int built_csr) {
+    CapLevel& c = st->lv[L];
+    const uint32_t n = *n_src;
+    if (st->stop || n == 0) {
+        st->stop = 1;
+        c.n_push = 0;
+        c.skip_direct = c.skip_early = 1;
+        return;
+    }
+    const bool dense = !built_csr || *act_src >= dense_min;
+    const bool early = dense && early_after_first && st->dense_count > 0;
+    c.n_push = dense ? 0u : n;
+    c.skip_direct = !(dense && !early);
+    c.skip_early = !(dense && early);
+    if (dense) ++st->dense_count;
 }
 
-constexpr int kGraphLevels = 32;
+// zero the frontier words a queue lists (its length read on the device), or the whole array when
+// the queue is long; nothing once the loop has stopped
+__global__ void k_clear_front_dev(const uint32_t* __restrict__ q, const uint32_t* n_dev, unsigned long long* word,
+                                  uint64_t V, const CapState* st) {
+    if (st->stop) return;
+    const uint32_t n = __ldcg(n_dev);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    if ((uint64_t)n > V / 32) {
+        for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += stride) word[v] = 0ull;
+    } else {
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) word[q[i]] = 0ull;
+    }
+}
 
 // MS-BFS over root entries already in b.entries (count in b.n_entries device word)
 // lev_filled: the level rows start as 0xFF (callers that hand them out as they are); otherwise
@@ -762,7 +809,6 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
     uint32_t* queue[2] = {s.q0.as<uint32_t>(), s.q1.as<uint32_t>()};
     unsigned long long* alive = b.alive.as<unsigned long long>();  // [0..1] per level parity, [2] all roots
     uint32_t* cnt = b.level_cnt.as<uint32_t>();  // [kGraphLevels + 1]
-    int* stop = reinterpret_cast<int*>(cnt + kGraphLevels + 1);
     unsigned long long* d_reach = s.counters.as<unsigned long long>() + 4;
     uint32_t* d_nq = reinterpret_cast<uint32_t*>(s.counters.as<unsigned long long>() + 2);
     unsigned long long* d_act = s.counters.as<unsigned long long>() + 3;
@@ -871,25 +917,137 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
 
     int sweeps = 0, pushes = 0;
     uint32_t lvl = 0;
+    // the host-driven level loop from level lvl on: the frontier (queue[lvl & 1]) lists n vertices
+    // with act out-edges; q0len / q1len are how many vertices queue[0] / queue[1] list
+    auto host_levels = [&](uint64_t n, unsigned long long act, uint64_t q0len, uint64_t q1len,
+                           int dense_levels) -> int {
+        struct {
+            uint32_t n;
+            uint32_t pad;
+            unsigned long long act;
+        } h;
+        uint64_t qlen[2] = {q0len, q1len};
+        while (n > 0) {
+            if (lvl >= 254) {
+                set_error("eg_msbfs: more than 254 levels");
+                return EG_ERR_UNSUPPORTED;
+            }
+            // the Gemini switch on the union frontier; EG_OPT_BFS_DIRECTION concerns single-root BFS
+            const bool dense = !g->built_csr || act >= g->E / (uint64_t)g->dense_div;
+            uint32_t nout = 0;
+            // a bitmap test before each gather pays only while the frontier is a small part of V
+            EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act, one_graph && dense_levels > 0,
+                                 qlen[(lvl & 1) ^ 1]));
+            if (dense) {
+                ++dense_levels;
+                EG_CUDA(cudaMemcpyAsync(&h, d_nq, 16, cudaMemcpyDeviceToHost, g->stream));
+                EG_CUDA(cudaStreamSynchronize(g->stream));
+                nout = h.n;
+                act = h.act;
+            } else {
+                ++pushes;
+            }
+            qlen[(lvl & 1) ^ 1] = nout;
+            ++sweeps;
+            n = nout;
+            ++lvl;
+        }
+        return EG_OK;
+    };
     if (g->use_cuda_graph) {
-        // init + kGraphLevels levels replayed as one CUDA graph; levels after an empty one stop at
-        // their first instruction (k_level_gate sets the flag the pull kernel checks)
+        // init + kGraphLevels levels replayed as one CUDA graph, each level choosing push or pull
+        // on the device (k_cap_decide); levels after an empty frontier do nothing
         const bool key_ok = b.graph_exec && b.graph_V == V && b.graph_lev == (lev != nullptr) &&
                             b.graph_entries >= n_entries && b.graph_nbits == nbits;
         if (!key_ok) {
             if (b.graph_exec) cudaGraphExecDestroy((cudaGraphExec_t)b.graph_exec);
             b.graph_exec = nullptr;
+            EG_TRY(b.cap.reserve(sizeof(CapState)));
+            const int P = g->partitions;
+            const uint64_t max_items = (V + 1) * (uint64_t)P;
+            const uint64_t max_tiles = (max_items + kScanTile - 1) / kScanTile;
+            EG_TRY(g->scan.desc.reserve(max_tiles * sizeof(uint64_t)));
+            EG_TRY(g->scan.counter.reserve(16));
             const bool prof = g->prof.enabled;
             g->prof.enabled = false;
             EG_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+            CapState* cs = b.cap.as<CapState>();
             int st = enqueue_init();
+            auto ok = [&](cudaError_t e) {
+                if (st == EG_OK && e != cudaSuccess) st = EG_ERR_CUDA;
+            };
+            ok(cudaMemsetAsync(cs, 0, sizeof(CapState), g->stream));
+            ok(cudaMemsetAsync(word[1], 0, 8 * V, g->stream));
+            const unsigned long long dense_min = g->E / (uint64_t)g->dense_div;
             for (uint32_t L = 0; st == EG_OK && L < (uint32_t)kGraphLevels; ++L) {
-                if (L > 0) {
-                    k_level_gate<<<1, 1, 0, g->stream>>>(cnt + L - 1, stop);
-                    st = cudaGetLastError() == cudaSuccess ? EG_OK : EG_ERR_CUDA;
+                const int c = L & 1, x = c ^ 1;
+                const uint32_t* n_cur = L == 0 ? d_nq : cnt + L - 1;
+                const unsigned long long* act_cur = L == 0 ? d_act : cs->act + L - 1;
+                k_cap_decide<<<1, 1, 0, g->stream>>>(cs, (int)L, n_cur, act_cur, dense_min, one_graph ? 1 : 0,
+                                                     g->built_csr ? 1 : 0);
+                ok(cudaGetLastError());
+                if (L >= 1) {  // the frontier words written two levels back (level 1: the roots)
+                    const uint32_t* n_old = L == 1 ? d_nq : cnt + L - 2;
+                    k_clear_front_dev<<<grid, 256, 0, g->stream>>>(queue[x], n_old, word[x], V, cs);
+                    ok(cudaGetLastError());
                 }
-                if (st == EG_OK)
-                    st = enqueue_level(L, 0, true, true, cnt + L, stop, nullptr, nullptr, one_graph && L >= 3, kUnknownQueue);
+                ok(cudaMemsetAsync(bm[x], 0, bm_bytes, g->stream));
+                // pull: the chunked sweep or the early-exit pair, whichever the level armed
+                {
+                    MsBfsPullOp op{word[c], bm[c], 1, visit, word[x], bm[x], alive + 2, &cs->lv[L].skip_direct};
+                    if (st == EG_OK) st = launch_pull_direct(g, op, "msbfs_pull", gather_adj, 16 * grid);
+                    uint32_t* d_nseg = reinterpret_cast<uint32_t*>(cnt + kGraphLevels + 2);
+                    ok(cudaMemsetAsync(d_nseg, 0, 4, g->stream));
+                    MsBuArgs ma{gather_adj, g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(), g->ncompressed - 1,
+                                (uint32_t)V, word[c], visit, word[x], bm[x], alive + 2,
+                                b.ms_seg.as<unsigned long long>(), d_nseg, &cs->lv[L].skip_early};
+                    k_ms_head<<<grid_for(ma.nitems, 256, grid), 256, 0, g->stream>>>(ma);
+                    ok(cudaGetLastError());
+                    k_ms_tail<<<grid, 256, 0, g->stream>>>(ma);
+                    ok(cudaGetLastError());
+                }
+                // push: scan of the queued lists' lengths and the rank-balanced expansion, sized on
+                // the device (zero items on pull levels)
+                if (g->built_csr) {
+                    const uint32_t* n_push = &cs->lv[L].n_push;
+                    uint64_t* ipref = s.qdeg.as<uint64_t>();
+                    ok(cudaMemsetAsync(g->scan.desc.ptr, 0, max_tiles * sizeof(uint64_t), g->stream));
+                    ok(cudaMemsetAsync(g->scan.counter.ptr, 0, 4, g->stream));
+                    LoadItemLen ld{queue[c], P, V + 1, g->csr_off.as<uint64_t>()};
+                    EpiItemRank ep{ipref, s.chunk_item.as<uint32_t>()};
+                    k_scan<<<(unsigned)std::min<uint64_t>(max_tiles, grid), kScanThreads, 0, g->stream>>>(
+                        ld, ep, max_items, g->scan.desc.as<uint64_t>(), g->scan.counter.as<uint32_t>(),
+                        g->err.as<int>(), &cs->push_total, kLookbackSpinCap, n_push, (uint32_t)P);
+                    ok(cudaGetLastError());
+                    PushArgs a;
+                    a.q = queue[c];
+                    a.nitems = 0;
+                    a.n_dev = n_push;
+                    a.total_dev = &cs->push_total;
+                    a.P = P;
+                    a.stride = V + 1;
+                    a.off = g->csr_off.as<uint64_t>();
+                    a.adj = g->csr_adj.as<uint32_t>();
+                    a.w = nullptr;
+                    a.ipref = ipref;
+                    a.chunk_item = s.chunk_item.as<uint32_t>();
+                    a.q_out = nullptr;
+                    a.n_out = nullptr;
+                    a.act_edges = nullptr;
+                    a.deg = nullptr;
+                    MsBfsPushOp pop{word[c], visit, word[x], bm[x]};
+                    k_push<MsBfsPushOp><<<kPersistentGrid, kPushThreads, 0, g->stream>>>(pop, a);
+                    ok(cudaGetLastError());
+                }
+                // the next frontier from its bitmap (either path), its out-edges and level bytes
+                k_bm_compact<<<grid_for(nwords, 256, grid), 256, 0, g->stream>>>(bm[x], nwords, queue[x], cnt + L,
+                                                                                cs->act + L, deg);
+                ok(cudaGetLastError());
+                if (lev) {
+                    k_queue_levels<<<grid, 256, 0, g->stream>>>(queue[x], cnt + L, word[x], lev, L + 1, nullptr,
+                                                                nullptr, nullptr);
+                    ok(cudaGetLastError());
+                }
             }
             cudaGraph_t graph = nullptr;
             cudaError_t e = cudaStreamEndCapture(g->stream, &graph);
@@ -911,27 +1069,24 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
             EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)b.graph_exec, g->stream));
         }
         std::vector<uint32_t> h(kGraphLevels);
+        CapState hs;
         EG_CUDA(cudaMemcpyAsync(h.data(), cnt, sizeof(uint32_t) * kGraphLevels, cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaMemcpyAsync(&hs, b.cap.ptr, sizeof(CapState), cudaMemcpyDeviceToHost, g->stream));
         EG_CUDA(cudaStreamSynchronize(g->stream));
         bool done = false;
         for (int L = 0; L < kGraphLevels && !done; ++L) {
             ++sweeps;
+            if (hs.lv[L].n_push) ++pushes;
             done = h[L] == 0;
         }
-        lvl = kGraphLevels;
-        uint32_t* d_new = cnt + kGraphLevels;
-        while (!done) {  // deeper than the captured levels
-            if (lvl >= 254) {
-                set_error("eg_msbfs: more than 254 levels");
-                return EG_ERR_UNSUPPORTED;
-            }
-            EG_TRY(enqueue_level(lvl, 0, true, true, d_new, stop, nullptr, nullptr, one_graph, kUnknownQueue));
-            ++sweeps;
-            uint32_t hn = 0;
-            EG_CUDA(cudaMemcpyAsync(&hn, d_new, 4, cudaMemcpyDeviceToHost, g->stream));
-            EG_CUDA(cudaStreamSynchronize(g->stream));
-            done = hn == 0;
-            ++lvl;
+        if (!done) {
+            // deeper than the captured levels: the host-driven loop takes over at level
+            // kGraphLevels (queue[0] lists level 31's output, queue[1] level 30's); the captured
+            // levels kept no running-root masks, so every root counts as running
+            lvl = kGraphLevels;
+            EG_CUDA(cudaMemcpyAsync(alive + (lvl & 1), &full, 8, cudaMemcpyHostToDevice, g->stream));
+            EG_TRY(host_levels(h[kGraphLevels - 1], hs.act[kGraphLevels - 1], h[kGraphLevels - 1], h[kGraphLevels - 2],
+                               hs.dense_count));
         }
     } else {
         EG_TRY(enqueue_init());
@@ -942,36 +1097,8 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         } h;
         EG_CUDA(cudaMemcpyAsync(&h, d_nq, 16, cudaMemcpyDeviceToHost, g->stream));
         EG_CUDA(cudaStreamSynchronize(g->stream));
-        uint64_t n = h.n;
-        unsigned long long act = h.act;
-        int dense_levels = 0;
-        // host lengths of what queue[0] / queue[1] list; queue[1] still holds an earlier call's
-        uint64_t qlen[2] = {n, kUnknownQueue};
-        while (n > 0) {
-            if (lvl >= 254) {
-                set_error("eg_msbfs: more than 254 levels");
-                return EG_ERR_UNSUPPORTED;
-            }
-            // the Gemini switch on the union frontier; EG_OPT_BFS_DIRECTION concerns single-root BFS
-            const bool dense = !g->built_csr || act >= g->E / (uint64_t)g->dense_div;
-            uint32_t nout = 0;
-            // a bitmap test before each gather pays only while the frontier is a small part of V
-            EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act, one_graph && dense_levels > 0,
-                                 qlen[(lvl & 1) ^ 1]));
-            if (dense) ++dense_levels;
-            if (dense) {
-                EG_CUDA(cudaMemcpyAsync(&h, d_nq, 16, cudaMemcpyDeviceToHost, g->stream));
-                EG_CUDA(cudaStreamSynchronize(g->stream));
-                nout = h.n;
-                act = h.act;
-            } else {
-                ++pushes;
-            }
-            qlen[(lvl & 1) ^ 1] = nout;
-            ++sweeps;
-            n = nout;
-            ++lvl;
-        }
+        // queue[1] still holds an earlier call's list: its length is unknown
+        EG_TRY(host_levels(h.n, h.act, h.n, kUnknownQueue, 0));
     }
     if (reach_out) {
         EG_CUDA(cudaMemsetAsync(d_reach, 0, 8, g->stream));

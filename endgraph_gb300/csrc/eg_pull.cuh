@@ -13,8 +13,10 @@
 namespace eg {
 
 // adj: the CSC source ids to gather through (default: the built CSC's)
+// max_grid (optional): a persistent grid that strides over the chunks instead of a CTA per chunk
 template <class Op>
-static int launch_pull_direct(eg_graph* g, const Op& op, const char* name, const uint32_t* adj = nullptr) {
+static int launch_pull_direct(eg_graph* g, const Op& op, const char* name, const uint32_t* adj = nullptr,
+                              unsigned max_grid = 0) {
     EngineState& s = g->eng;
     if (s.pull_nchunks == 0) return EG_OK;
     const uint64_t nitems = g->ncompressed - 1;
@@ -22,7 +24,8 @@ static int launch_pull_direct(eg_graph* g, const Op& op, const char* name, const
     const size_t smem = 6 * ((size_t)kPullChunk + g->partitions + 3);
     EG_CUDA(cudaFuncSetAttribute(k_pull_direct<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     Timed t(&g->prof, g->stream, name);
-    k_pull_direct<Op><<<(unsigned)s.pull_nchunks, kPullThreads, smem, g->stream>>>(
+    const unsigned grid = max_grid ? (unsigned)std::min<uint64_t>(s.pull_nchunks, max_grid) : (unsigned)s.pull_nchunks;
+    k_pull_direct<Op><<<grid, kPullThreads, smem, g->stream>>>(
         op, adj ? adj : g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(),
         s.pull_chunk_item.as<uint32_t>(), g->E, nitems, g->V);
     EG_CHECK_LAUNCH(name);

@@ -180,7 +180,9 @@ int eg_sssp(eg_graph* g, uint32_t root, float* dist, int where);
  * does (core/graph.hpp:1496-1498), 2 forces pull.  Results are identical in every mode.  The
  * bit-parallel BFS always switches on its union frontier with the same divisor.
  * EG_OPT_CUDA_GRAPH: 1 replays the batched-BFS level loop (eg_msbfs, eg_msbfs_graphs) as one
- * captured CUDA graph of 32 levels instead of one host round trip per level. */
+ * captured CUDA graph of 16 levels, each choosing push or pull on the device from its frontier's
+ * out-edges (the same switch as the host loop), instead of one host round trip per level; deeper
+ * traversals continue from the host. */
 enum {
     EG_OPT_BFS_DIRECTION = 1,
     EG_OPT_DENSE_DIVISOR = 2,

@@ -3,8 +3,8 @@
 // (endgraph_gb300_engine.cuh).  CUDA C++ for sm_103a; no host state.
 //
 //  * k_scan: single-pass prefix scan (decoupled look-back) over u32 items with u64 sums.  Each
-//    256-thread CTA takes the next 4096-item tile from a ticket counter (so every tile it waits on
-//    belongs to a CTA that is already running), scans it in shared memory, publishes its
+//    256-thread CTA takes 4096-item tiles from a ticket counter until they run out (so every tile
+//    it waits on belongs to a CTA that is already running), scans each in shared memory, publishes its
 //    aggregate, looks back over predecessor descriptors with warp 0, publishes its inclusive prefix
 //    and hands (index, exclusive prefix, value) of every item to an epilogue functor.  Descriptor:
 //    status in bits 63..62 (1 aggregate, 2 inclusive), value in 61..0.  The look-back spin is
@@ -74,96 +74,111 @@ __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
 template <class Load, class Epi>
 __global__ void __launch_bounds__(kScanThreads) k_scan(Load load, Epi epi, uint64_t n, uint64_t* desc,
                                                         uint32_t* ticket, int* err, uint64_t* total_out,
-                                                        uint32_t spin_cap) {
+                                                        uint32_t spin_cap, const uint32_t* n_dev = nullptr,
+                                                        uint32_t n_mult = 1) {
     __shared__ uint32_t s_vals[kScanTile + kScanTile / 32];
     __shared__ uint64_t s_warp[kScanThreads / 32];
     __shared__ uint64_t s_prefix;
     __shared__ uint32_t s_tile;
-    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    const uint64_t base = (uint64_t)tile * kScanTile;
-#pragma unroll
-    for (int j = 0; j < kScanItems; ++j) {
-        uint32_t li = threadIdx.x + j * kScanThreads;
-        uint64_t gi = base + li;
-        s_vals[li + li / 32] = gi < n ? load(gi) : 0u;
+    // n_dev: the item count is read on the device (at most n), for launches whose grid is sized for
+    // the largest count (a captured graph); the tiles past it leave at once.  No tile waits on a
+    // later tile, and tile 0 always runs, so the total is written even for zero items.
+    if (n_dev) {
+        const uint64_t nd = (uint64_t)__ldcg(n_dev) * n_mult;
+        n = nd < n ? nd : n;
     }
-    __syncthreads();
-    uint32_t v[kScanItems];
-    uint64_t tsum = 0;
+    // a CTA takes tiles by ticket until they run out, so a grid smaller than the tile count works
+    // too (tiles are taken in order by running CTAs, so every wait is on a running tile)
+    while (true) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        const uint64_t base = (uint64_t)tile * kScanTile;
+        if (tile > 0 && base >= n) return;
 #pragma unroll
-    for (int j = 0; j < kScanItems; ++j) {
-        uint32_t li = threadIdx.x * kScanItems + j;
-        v[j] = s_vals[li + li / 32];
-        tsum += v[j];
-    }
-    // block exclusive scan of per-thread sums
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint64_t inc = tsum;
+        for (int j = 0; j < kScanItems; ++j) {
+            uint32_t li = threadIdx.x + j * kScanThreads;
+            uint64_t gi = base + li;
+            s_vals[li + li / 32] = gi < n ? load(gi) : 0u;
+        }
+        __syncthreads();
+        uint32_t v[kScanItems];
+        uint64_t tsum = 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint64_t y = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += y;
-    }
-    if (lane == 31) s_warp[warp] = inc;
-    __syncthreads();
-    uint64_t warp_base = 0, tile_agg = 0;
+        for (int j = 0; j < kScanItems; ++j) {
+            uint32_t li = threadIdx.x * kScanItems + j;
+            v[j] = s_vals[li + li / 32];
+            tsum += v[j];
+        }
+        // block exclusive scan of per-thread sums
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint64_t inc = tsum;
 #pragma unroll
-    for (int w = 0; w < kScanThreads / 32; ++w) {
-        uint64_t x = s_warp[w];
-        if (w < warp) warp_base += x;
-        tile_agg += x;
-    }
-    const uint64_t texcl = warp_base + inc - tsum;
-    // look-back
-    if (warp == 0) {
-        uint64_t prefix = 0;
-        if (tile == 0) {
-            if (lane == 0) atomicExch((unsigned long long*)&desc[0], (unsigned long long)(kStInc | tile_agg));
-        } else {
-            if (lane == 0) atomicExch((unsigned long long*)&desc[tile], (unsigned long long)(kStAgg | tile_agg));
-            int64_t pred = (int64_t)tile - 1;
-            uint32_t spins = 0;
-            bool timed_out = false;
-            while (true) {
-                int64_t idx = pred - lane;
-                uint64_t d = idx >= 0 ? ld_volatile_u64(&desc[idx]) : kStInc;
-                uint32_t st = (uint32_t)(d >> 62);
-                if (__any_sync(0xffffffffu, st == 0)) {
-                    if (++spins > spin_cap) {
-                        timed_out = true;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) s_warp[warp] = inc;
+        __syncthreads();
+        uint64_t warp_base = 0, tile_agg = 0;
+#pragma unroll
+        for (int w = 0; w < kScanThreads / 32; ++w) {
+            uint64_t x = s_warp[w];
+            if (w < warp) warp_base += x;
+            tile_agg += x;
+        }
+        const uint64_t texcl = warp_base + inc - tsum;
+        // look-back
+        if (warp == 0) {
+            uint64_t prefix = 0;
+            if (tile == 0) {
+                if (lane == 0) atomicExch((unsigned long long*)&desc[0], (unsigned long long)(kStInc | tile_agg));
+            } else {
+                if (lane == 0) atomicExch((unsigned long long*)&desc[tile], (unsigned long long)(kStAgg | tile_agg));
+                int64_t pred = (int64_t)tile - 1;
+                uint32_t spins = 0;
+                bool timed_out = false;
+                while (true) {
+                    int64_t idx = pred - lane;
+                    uint64_t d = idx >= 0 ? ld_volatile_u64(&desc[idx]) : kStInc;
+                    uint32_t st = (uint32_t)(d >> 62);
+                    if (__any_sync(0xffffffffu, st == 0)) {
+                        if (++spins > spin_cap) {
+                            timed_out = true;
+                            break;
+                        }
+                        __nanosleep(64);
+                        continue;
+                    }
+                    uint32_t inc_mask = __ballot_sync(0xffffffffu, st == 2);
+                    uint64_t val = d & kValMask;
+                    if (idx < 0) val = 0;
+                    if (inc_mask) {
+                        int k = __ffs(inc_mask) - 1;
+                        prefix += warp_sum_u64(lane <= k ? val : 0);
                         break;
                     }
-                    __nanosleep(64);
-                    continue;
+                    prefix += warp_sum_u64(val);
+                    pred -= 32;
                 }
-                uint32_t inc_mask = __ballot_sync(0xffffffffu, st == 2);
-                uint64_t val = d & kValMask;
-                if (idx < 0) val = 0;
-                if (inc_mask) {
-                    int k = __ffs(inc_mask) - 1;
-                    prefix += warp_sum_u64(lane <= k ? val : 0);
-                    break;
-                }
-                prefix += warp_sum_u64(val);
-                pred -= 32;
+                if (timed_out && lane == 0) atomicExch(err, 1);
+                if (lane == 0)
+                    atomicExch((unsigned long long*)&desc[tile], (unsigned long long)(kStInc | ((prefix + tile_agg) & kValMask)));
             }
-            if (timed_out && lane == 0) atomicExch(err, 1);
-            if (lane == 0)
-                atomicExch((unsigned long long*)&desc[tile], (unsigned long long)(kStInc | ((prefix + tile_agg) & kValMask)));
+            if (lane == 0) s_prefix = prefix;
         }
-        if (lane == 0) s_prefix = prefix;
-    }
-    __syncthreads();
-    uint64_t run = s_prefix + texcl;
-    const uint64_t first = base + (uint64_t)threadIdx.x * kScanItems;
+        __syncthreads();
+        uint64_t run = s_prefix + texcl;
+        const uint64_t first = base + (uint64_t)threadIdx.x * kScanItems;
 #pragma unroll
-    for (int j = 0; j < kScanItems; ++j) {
-        if (first + j < n) epi(first + j, run, v[j]);
-        run += v[j];
+        for (int j = 0; j < kScanItems; ++j) {
+            if (first + j < n) epi(first + j, run, v[j]);
+            run += v[j];
+        }
+        if (total_out && threadIdx.x == 0 && base + kScanTile >= n) *total_out = s_prefix + tile_agg;
+        if (base + kScanTile >= n) return;  // the last tile: nothing left to take
+        __syncthreads();                    // s_tile, s_vals and s_prefix are reused by the next tile
     }
-    if (total_out && threadIdx.x == 0 && base + kScanTile >= n) *total_out = s_prefix + tile_agg;
 }
 
 
@@ -346,95 +361,99 @@ __global__ void __launch_bounds__(kPullThreads) k_pull_direct(Op op, const uint3
     using Acc = typename Op::Acc;
     if (op.stopped()) return;
     extern __shared__ __align__(16) unsigned char s_raw[];
-    const uint64_t c = blockIdx.x;
-    const uint64_t e0 = c * kPullChunk;
-    const uint64_t e1 = e0 + kPullChunk < E ? e0 + kPullChunk : E;
-    const uint32_t i0 = chunk_item[c];
-    const uint32_t j = chunk_item[c + 1];
-    const uint32_t iend = (j < nitems && cidx[j] < e1) ? j + 1 : j;
-    const int nit = (int)(iend - i0);
-    uint32_t* s_v = reinterpret_cast<uint32_t*>(s_raw);    // destination, or ~0u when filtered out
-    uint16_t* s_idx = reinterpret_cast<uint16_t*>(s_v + nit);  // nit + 1 boundaries relative to e0
-    for (int k = threadIdx.x; k <= nit; k += blockDim.x) {
-        const uint64_t x = cidx[i0 + k];
-        s_idx[k] = (uint16_t)(x <= e0 ? 0u : (x >= e1 ? (uint32_t)(e1 - e0) : (uint32_t)(x - e0)));
-        if (k < nit) {
-            const uint32_t v = cvert[i0 + k];
-            s_v[k] = (v < V && op.item_active(v)) ? v : 0xFFFFFFFFu;
-        }
-    }
-    __syncthreads();
-    const uint64_t eb = e0 + (uint64_t)threadIdx.x * kPullPerThread;
-    const uint32_t rb = (uint32_t)(eb - e0);
-    int fin_key = 0x7fffffff;
-    Acc fin = op.identity();
-    if (eb < e1) {
-        int lo = 0, hi = nit;
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (s_idx[mid] <= rb) lo = mid; else hi = mid;
-        }
-        const uint64_t ee = eb + kPullPerThread < e1 ? eb + kPullPerThread : e1;
-        const uint32_t re = (uint32_t)(ee - e0);
-        uint32_t act = 0;
-        {
-            int k = lo;
-            uint32_t nb = s_idx[k + 1];
-#pragma unroll
-            for (int q = 0; q < kPullPerThread; ++q) {
-                const uint32_t e = rb + q;
-                if (e < re) {
-                    while (e >= nb) nb = s_idx[++k + 1];
-                    if (s_v[k] != 0xFFFFFFFFu) act |= 1u << q;
-                }
+    // one chunk per CTA when launched with a CTA per chunk; a smaller (persistent) grid strides
+    const uint64_t nchunks = (E + kPullChunk - 1) / kPullChunk;
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint64_t e0 = c * kPullChunk;
+        const uint64_t e1 = e0 + kPullChunk < E ? e0 + kPullChunk : E;
+        const uint32_t i0 = chunk_item[c];
+        const uint32_t j = chunk_item[c + 1];
+        const uint32_t iend = (j < nitems && cidx[j] < e1) ? j + 1 : j;
+        const int nit = (int)(iend - i0);
+        uint32_t* s_v = reinterpret_cast<uint32_t*>(s_raw);    // destination, or ~0u when filtered out
+        uint16_t* s_idx = reinterpret_cast<uint16_t*>(s_v + nit);  // nit + 1 boundaries relative to e0
+        for (int k = threadIdx.x; k <= nit; k += blockDim.x) {
+            const uint64_t x = cidx[i0 + k];
+            s_idx[k] = (uint16_t)(x <= e0 ? 0u : (x >= e1 ? (uint32_t)(e1 - e0) : (uint32_t)(x - e0)));
+            if (k < nit) {
+                const uint32_t v = cvert[i0 + k];
+                s_v[k] = (v < V && op.item_active(v)) ? v : 0xFFFFFFFFu;
             }
         }
-        if (act) {
-            uint32_t ids[kPullPerThread];
-            if (ee - eb == kPullPerThread) {
-                const uint4* p = reinterpret_cast<const uint4*>(adj + eb);
-#pragma unroll
-                for (int q = 0; q < kPullPerThread / 4; ++q) {
-                    const uint4 x = __ldcs(p + q);
-                    ids[4 * q] = x.x; ids[4 * q + 1] = x.y; ids[4 * q + 2] = x.z; ids[4 * q + 3] = x.w;
-                }
-            } else {
-#pragma unroll
-                for (int q = 0; q < kPullPerThread; ++q) ids[q] = eb + q < ee ? adj[eb + q] : 0u;
+        __syncthreads();
+        const uint64_t eb = e0 + (uint64_t)threadIdx.x * kPullPerThread;
+        const uint32_t rb = (uint32_t)(eb - e0);
+        int fin_key = 0x7fffffff;
+        Acc fin = op.identity();
+        if (eb < e1) {
+            int lo = 0, hi = nit;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (s_idx[mid] <= rb) lo = mid; else hi = mid;
             }
-            Acc vals[kPullPerThread];
+            const uint64_t ee = eb + kPullPerThread < e1 ? eb + kPullPerThread : e1;
+            const uint32_t re = (uint32_t)(ee - e0);
+            uint32_t act = 0;
+            {
+                int k = lo;
+                uint32_t nb = s_idx[k + 1];
 #pragma unroll
-            for (int q = 0; q < kPullPerThread; ++q) vals[q] = (act >> q) & 1u ? op.gather(ids[q]) : op.identity();
-            int k = lo;
-            uint32_t nb = s_idx[k + 1];
-            Acc a = op.identity();
-#pragma unroll
-            for (int q = 0; q < kPullPerThread; ++q) {
-                const uint32_t e = rb + q;
-                if (e < re) {
-                    while (e >= nb) {
-                        if (a != op.identity()) op.finish_direct(s_v[k], a);
-                        a = op.identity();
-                        ++k;
-                        nb = s_idx[k + 1];
+                for (int q = 0; q < kPullPerThread; ++q) {
+                    const uint32_t e = rb + q;
+                    if (e < re) {
+                        while (e >= nb) nb = s_idx[++k + 1];
+                        if (s_v[k] != 0xFFFFFFFFu) act |= 1u << q;
                     }
-                    a = op.combine(a, vals[q]);
                 }
             }
-            fin_key = k;
-            fin = a;
-        }
-    }
-    const int lane = threadIdx.x & 31;
+            if (act) {
+                uint32_t ids[kPullPerThread];
+                if (ee - eb == kPullPerThread) {
+                    const uint4* p = reinterpret_cast<const uint4*>(adj + eb);
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const Acc vo = __shfl_up_sync(0xffffffffu, fin, o);
-        const int ko = __shfl_up_sync(0xffffffffu, fin_key, o);
-        if (lane >= o && ko == fin_key) fin = op.combine(fin, vo);
+                    for (int q = 0; q < kPullPerThread / 4; ++q) {
+                        const uint4 x = __ldcs(p + q);
+                        ids[4 * q] = x.x; ids[4 * q + 1] = x.y; ids[4 * q + 2] = x.z; ids[4 * q + 3] = x.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < kPullPerThread; ++q) ids[q] = eb + q < ee ? adj[eb + q] : 0u;
+                }
+                Acc vals[kPullPerThread];
+#pragma unroll
+                for (int q = 0; q < kPullPerThread; ++q) vals[q] = (act >> q) & 1u ? op.gather(ids[q]) : op.identity();
+                int k = lo;
+                uint32_t nb = s_idx[k + 1];
+                Acc a = op.identity();
+#pragma unroll
+                for (int q = 0; q < kPullPerThread; ++q) {
+                    const uint32_t e = rb + q;
+                    if (e < re) {
+                        while (e >= nb) {
+                            if (a != op.identity()) op.finish_direct(s_v[k], a);
+                            a = op.identity();
+                            ++k;
+                            nb = s_idx[k + 1];
+                        }
+                        a = op.combine(a, vals[q]);
+                    }
+                }
+                fin_key = k;
+                fin = a;
+            }
+        }
+        const int lane = threadIdx.x & 31;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const Acc vo = __shfl_up_sync(0xffffffffu, fin, o);
+            const int ko = __shfl_up_sync(0xffffffffu, fin_key, o);
+            if (lane >= o && ko == fin_key) fin = op.combine(fin, vo);
+        }
+        const int knext = __shfl_down_sync(0xffffffffu, fin_key, 1);
+        if (fin_key != 0x7fffffff && (lane == 31 || knext != fin_key) && fin != op.identity())
+            op.finish_direct(s_v[fin_key], fin);
+        if (c + gridDim.x < nchunks) __syncthreads();  // the next chunk reuses the staged entries
     }
-    const int knext = __shfl_down_sync(0xffffffffu, fin_key, 1);
-    if (fin_key != 0x7fffffff && (lane == 31 || knext != fin_key) && fin != op.identity())
-        op.finish_direct(s_v[fin_key], fin);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -517,6 +536,10 @@ __device__ __forceinline__ void append_block_deg(bool act, uint32_t w, uint32_t*
 struct PushArgs {
     const uint32_t* q;
     uint64_t nitems;
+    // optional: the queue length read on the device (items = *n_dev * P) and the edge total the
+    // scan wrote at *total_dev, for launches made before the count is known on the host
+    const uint32_t* n_dev = nullptr;
+    const uint64_t* total_dev = nullptr;
     int P;
     uint64_t stride;
     const uint64_t* off;
@@ -549,7 +572,11 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Op op, PushArgs a) {
     std::conditional_t<kReduce, Val, int> acc{};
     __shared__ uint32_t s_cnt[kPushThreads / 32 + 1];
     unsigned long long my_act = 0;  // out-edges of the vertices this thread activated
-    const uint64_t T = a.ipref[a.nitems];
+    if (a.n_dev) a.nitems = (uint64_t)__ldcg(a.n_dev) * (uint64_t)a.P;
+    const uint64_t T = a.total_dev ? __ldcg(a.total_dev) : a.ipref[a.nitems];
+    // item starts; the end of the last item is the total (the scan writes it at ipref[nitems], or
+    // at *total_dev when the count came from the device)
+    auto pref = [&](uint64_t i) -> uint64_t { return i >= a.nitems ? T : a.ipref[i]; };
     const uint64_t nchunks = (T + kPushChunk - 1) / kPushChunk;
     for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         uint32_t got[kPushPerThread];  // activated vertices of this thread's edges (slot q: edge q)
@@ -568,7 +595,7 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Op op, PushArgs a) {
             }
         }
         uint64_t it = lo;
-        uint64_t ibeg = a.ipref[it], iend = a.ipref[it + 1];
+        uint64_t ibeg = pref(it), iend = pref(it + 1);
         uint32_t u = a.q[it / a.P];
         uint64_t lbase = a.off[(it % a.P) * a.stride + u];
         auto pay = op.payload(u);
@@ -581,7 +608,7 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Op op, PushArgs a) {
                 while (e >= iend) {
                     ++it;
                     ibeg = iend;
-                    iend = a.ipref[it + 1];
+                    iend = pref(it + 1);
                     u = a.q[it / a.P];
                     lbase = a.off[(it % a.P) * a.stride + u];
                     pay = op.payload(u);

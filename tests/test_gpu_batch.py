@@ -60,7 +60,8 @@ def test_msbfs_renumbered_gathers(eg_lib, direction_div):
 
 @pytest.mark.parametrize("cuda_graph", [0, 1])
 def test_msbfs_cuda_graph_mode(eg_lib, cuda_graph):
-    """The captured 32-level loop gives the same levels as the host-driven loop."""
+    """The captured 32-level loop (each level choosing push or pull on the device) gives the same
+    levels as the host-driven loop, and takes both directions as the host loop does."""
     import endgraph_gb300 as eg
     V, E = 1 << 13, 1 << 16
     src, dst, _ = rmat_graph(V, E, 97)
@@ -72,6 +73,8 @@ def test_msbfs_cuda_graph_mode(eg_lib, cuda_graph):
         for rep in range(2):  # the second call replays the cached graph
             levels, _ = g.msbfs(roots[rep * 8:] if rep else roots)
             use = roots[rep * 8:] if rep else roots
+            run = g.last_run()
+            assert run["push"] > 0 and run["pull"] > 0  # both directions, chosen on the device when captured
             for s in (0, 5, len(use) - 1):
                 ref = oracle.bfs_levels(csr["off"][0], csr["adj"], V, int(use[s]))
                 assert np.array_equal(levels[s], np.where(ref == oracle.UNREACHED, 255, ref).astype(np.uint8))

@@ -76,7 +76,7 @@ def test_hub_in_list_longer_than_a_segment(eg_lib, direction):
 
 
 def test_deep_path(eg_lib):
-    """A 200-vertex chain: deeper than the 32 captured levels; 254 levels are the u8 limit of MS-BFS."""
+    """A 200-vertex chain: deeper than the 16 captured levels; 254 levels are the u8 limit of MS-BFS."""
     import endgraph_gb300 as eg
     n = 200
     src = np.arange(n - 1, dtype=np.uint32)
