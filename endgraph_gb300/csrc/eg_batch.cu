@@ -38,8 +38,9 @@ constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 // the frontier bitmap is not gathered at all.  The traversal kernels only set bits; the next
 // frontier is then listed once (k_bm_compact) and its level bytes written from that list
 // (k_queue_levels), so no traversal thread loops over the bits of a word.
+// L2-coherent (.cg): the persistent traversal reads bitmaps that the same launch wrote
 __device__ __forceinline__ bool bm_has(const unsigned long long* bm, uint32_t v) {
-    return (__ldg(bm + (v >> 6)) >> (v & 63)) & 1ull;
+    return (__ldcg(bm + (v >> 6)) >> (v & 63)) & 1ull;
 }
 
 struct MsBfsPullOp {  // k_pull_direct operator
@@ -102,8 +103,7 @@ __device__ __forceinline__ void ms_apply(const MsBuArgs& a, uint32_t v, unsigned
     if (nb && atomicOr(a.next + v, nb) == 0ull) atomicOr(a.next_bm + (v >> 6), 1ull << (v & 63));
 }
 
-__global__ void __launch_bounds__(256) k_ms_head(MsBuArgs a) {
-    if (a.stop && *(volatile const int*)a.stop) return;
+__device__ __forceinline__ void ms_head_work(const MsBuArgs& a) {
     const int lane = threadIdx.x & 31;
     const unsigned long long al = __ldg(a.alive);
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -145,8 +145,12 @@ __global__ void __launch_bounds__(256) k_ms_head(MsBuArgs a) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_ms_tail(MsBuArgs a) {
+__global__ void __launch_bounds__(256) k_ms_head(MsBuArgs a) {
     if (a.stop && *(volatile const int*)a.stop) return;
+    ms_head_work(a);
+}
+
+__device__ __forceinline__ void ms_tail_work(const MsBuArgs& a) {
     const uint32_t n = __ldcg(a.nseg);
     const int lane = threadIdx.x & 31;
     const unsigned long long al = __ldg(a.alive);
@@ -174,6 +178,11 @@ __global__ void __launch_bounds__(256) k_ms_tail(MsBuArgs a) {
     }
 }
 
+__global__ void __launch_bounds__(256) k_ms_tail(MsBuArgs a) {
+    if (a.stop && *(volatile const int*)a.stop) return;
+    ms_tail_work(a);
+}
+
 struct MsBfsPushOp {
     const unsigned long long* front;
     unsigned long long* visit;
@@ -195,11 +204,11 @@ struct MsBfsPushOp {
 // the roots whose traversal is still running
 // With new_id, the words are also copied to renumbered positions (next_r[new_id[v]]) for the pull
 // gathers that go through the renumbered CSC sources.
-__global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n_dev,
-                               const unsigned long long* __restrict__ next, uint8_t* levels, uint32_t lvl,
-                               unsigned long long* alive_out, const uint32_t* __restrict__ new_id,
-                               unsigned long long* __restrict__ next_r) {
-    const uint32_t n = __ldcg(n_dev);
+__device__ __forceinline__ void queue_levels_work(const uint32_t* __restrict__ q, uint32_t n,
+                                                  const unsigned long long* __restrict__ next, uint8_t* levels,
+                                                  uint32_t lvl, unsigned long long* alive_out,
+                                                  const uint32_t* __restrict__ new_id,
+                                                  unsigned long long* __restrict__ next_r) {
     const uint32_t sub = threadIdx.x & 1u;
     const uint32_t fill = (lvl & 0xFFu) * 0x01010101u;
     unsigned long long orr = 0;
@@ -232,6 +241,13 @@ __global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) orr |= __shfl_xor_sync(0xffffffffu, orr, o);
     if ((threadIdx.x & 31) == 0 && orr) atomicOr(alive_out, orr);
+}
+
+__global__ void k_queue_levels(const uint32_t* __restrict__ q, const uint32_t* n_dev,
+                               const unsigned long long* __restrict__ next, uint8_t* levels, uint32_t lvl,
+                               unsigned long long* alive_out, const uint32_t* __restrict__ new_id,
+                               unsigned long long* __restrict__ next_r) {
+    queue_levels_work(q, __ldcg(n_dev), next, levels, lvl, alive_out, new_id, next_r);
 }
 
 // zero the frontier words (and their renumbered copies) of the vertices a queue lists: the only
@@ -659,7 +675,8 @@ int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E) {
 struct BatchState {
     DevBuf a64, b64, c64, lev, rows0, rows1, heavy, tmp_out, seeds, wn_csc, wn_csr, s_out, gA, row_of, ck, seg;
     DevBuf ch0, ch1, flag, level_cnt, entries, n_entries, bm0, bm1, alive, ms_seg;
-    DevBuf cap;  // captured level loop: per-level direction decisions and frontier edge counts
+    DevBuf cap;      // captured level loop: per-level direction decisions and frontier edge counts
+    DevBuf persist;  // persistent traversal: per-level counts, barrier words, error flag
     DevBuf wr0, wr1;  // frontier words in renumbered order (pull gathers through renumbered sources)
     RowTasks csc_tasks, csr_tasks;
     bool csc_ready = false, csr_ready = false;
@@ -793,6 +810,171 @@ __global__ void k_clear_front_dev(const uint32_t* __restrict__ q, const uint32_t
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// The whole bit-parallel traversal in one persistent launch (EG_OPT_BATCH_LAUNCH = 1): every
+// resident CTA runs every level, phase by phase, with a grid barrier between phases -- the same
+// phases as the host-driven loop (clear, push or pull by the E / divisor switch, list the next
+// frontier, level bytes), with the switch and the queue lengths read on the device.  A launch
+// that could not keep all its CTAs resident is refused by the cooperative launch, and every
+// barrier wait is bounded: on exhaustion the error flag is raised and the kernel returns.
+constexpr int kMaxLevels = 256;
+constexpr uint32_t kBarrierSpinCap = 1u << 22;
+
+struct PersistWords {
+    uint32_t cnt[kMaxLevels];          // queue length produced by level L
+    unsigned long long act[kMaxLevels];  // out-edges of that queue
+    uint32_t nseg[kMaxLevels];         // early-exit segments of level L
+    uint32_t ticket[kMaxLevels];       // scan tile tickets of level L
+    uint32_t chunk[kMaxLevels];        // pull chunk tickets of level L
+    uint64_t total[kMaxLevels];        // push edges of level L
+    unsigned bar_count, bar_gen;
+    int err;
+    uint32_t levels, pushes;
+};
+
+struct MsPersistArgs {
+    uint64_t V, nwords;
+    int P;
+    const uint64_t* csr_off;
+    const uint32_t* csr_adj;
+    const uint32_t* gather_adj;
+    const uint64_t* cidx;
+    const uint32_t* cvert;
+    uint64_t nitems;
+    const uint32_t* pull_chunk_item;
+    uint64_t E;
+    const uint32_t* deg;
+    unsigned long long* visit;
+    unsigned long long* word0;
+    unsigned long long* word1;
+    unsigned long long* bm0;
+    unsigned long long* bm1;
+    uint32_t* q0;
+    uint32_t* q1;
+    const unsigned long long* alive_all;
+    uint8_t* lev;
+    unsigned long long* ms_seg;
+    uint64_t* desc;
+    uint64_t* ipref;
+    uint32_t* push_chunk_item;
+    const uint32_t* init_n;
+    const unsigned long long* init_act;
+    unsigned long long dense_min;
+    int early_after_first, built_csr;
+    PersistWords* w;
+};
+
+// bounded grid barrier (all CTAs resident): false when a wait ran out
+__device__ __forceinline__ bool grid_barrier(PersistWords* w) {
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        const unsigned nblocks = gridDim.x;
+        const unsigned gen = *(volatile unsigned*)&w->bar_gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&w->bar_count, 1u) == nblocks - 1) {
+            atomicExch(&w->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&w->bar_gen, 1u);
+        } else {
+            uint32_t spins = 0;
+            while (*(volatile unsigned*)&w->bar_gen == gen) {
+                if (++spins > kBarrierSpinCap || *(volatile int*)&w->err) {
+                    atomicExch(&w->err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__global__ void __launch_bounds__(256, 4) k_msbfs_persistent(MsPersistArgs a) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    PersistWords* w = a.w;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t n = __ldcg(a.init_n);
+    unsigned long long act = __ldcg(a.init_act);
+    int dense_count = 0;
+    for (uint32_t L = 0; L < 254 && n > 0; ++L) {
+        const int c = L & 1;
+        unsigned long long* front = c ? a.word1 : a.word0;
+        unsigned long long* next = c ? a.word0 : a.word1;
+        const unsigned long long* front_bm = c ? a.bm1 : a.bm0;
+        unsigned long long* next_bm = c ? a.bm0 : a.bm1;
+        const uint32_t* q = c ? a.q1 : a.q0;
+        uint32_t* q_next = c ? a.q0 : a.q1;
+        const bool dense = !a.built_csr || act >= a.dense_min;
+        const bool early = dense && a.early_after_first && dense_count > 0;
+        // clear: the next-frontier words (set two levels back, listed by q_next; level 0: all of
+        // them), its bitmap, and the scan descriptors of a push level
+        {
+            const uint32_t n_old = L == 0 ? 0xFFFFFFFFu : (L == 1 ? __ldcg(a.init_n) : __ldcg(&w->cnt[L - 2]));
+            if (n_old > a.V / 32) {
+                for (uint64_t v = tid; v < a.V; v += stride) next[v] = 0ull;
+            } else {
+                for (uint64_t i = tid; i < n_old; i += stride) next[q_next[i]] = 0ull;
+            }
+            for (uint64_t i = tid; i < a.nwords; i += stride) next_bm[i] = 0ull;
+            if (!dense) {
+                const uint64_t tiles = ((uint64_t)n * a.P + kScanTile - 1) / kScanTile + 1;
+                for (uint64_t i = tid; i < tiles; i += stride) a.desc[i] = 0ull;
+            }
+        }
+        if (!grid_barrier(w)) return;
+        if (dense && early) {
+            MsBuArgs ma{a.gather_adj, a.cidx, a.cvert, a.nitems, (uint32_t)a.V, front, a.visit, next, next_bm,
+                        a.alive_all, a.ms_seg, &w->nseg[L], nullptr};
+            ms_head_work(ma);
+            if (!grid_barrier(w)) return;
+            ms_tail_work(ma);
+        } else if (dense) {
+            MsBfsPullOp op{front, front_bm, (uint64_t)n * 16 < a.V ? 1 : 0, a.visit, next, next_bm, a.alive_all, nullptr};
+            pull_direct_chunks(op, a.gather_adj, a.cidx, a.cvert, a.pull_chunk_item, a.E, a.nitems, (uint32_t)a.V,
+                               s_raw, &w->chunk[L]);
+        } else {
+            const uint64_t items = (uint64_t)n * a.P;
+            scan_tiles(LoadItemLen{q, a.P, a.V + 1, a.csr_off}, EpiItemRank{a.ipref, a.push_chunk_item}, items, a.desc,
+                       &w->ticket[L], &w->err, &w->total[L], kLookbackSpinCap);
+            if (!grid_barrier(w)) return;
+            PushArgs pa;
+            pa.q = q;
+            pa.nitems = items;
+            pa.total_dev = &w->total[L];
+            pa.P = a.P;
+            pa.stride = a.V + 1;
+            pa.off = a.csr_off;
+            pa.adj = a.csr_adj;
+            pa.w = nullptr;
+            pa.ipref = a.ipref;
+            pa.chunk_item = a.push_chunk_item;
+            pa.q_out = nullptr;
+            pa.n_out = nullptr;
+            pa.act_edges = nullptr;
+            pa.deg = nullptr;
+            push_chunks(MsBfsPushOp{front, a.visit, next, next_bm}, pa);
+        }
+        if (!grid_barrier(w)) return;
+        bm_compact_words(next_bm, a.nwords, q_next, &w->cnt[L], &w->act[L], a.deg);
+        if (!grid_barrier(w)) return;
+        n = __ldcg(&w->cnt[L]);
+        act = __ldcg(&w->act[L]);
+        if (dense) ++dense_count;
+        if (a.lev) queue_levels_work(q_next, n, next, a.lev, L + 1, nullptr, nullptr, nullptr);
+        if (tid == 0) {
+            w->levels = L + 1;
+            w->pushes += dense ? 0u : 1u;
+        }
+    }
+}
+
 // MS-BFS over root entries already in b.entries (count in b.n_entries device word)
 // lev_filled: the level rows start as 0xFF (callers that hand them out as they are); otherwise
 // their unreached bytes are left as they are and masked by k_levels_out
@@ -820,7 +1002,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
     constexpr uint64_t kUnknownQueue = ~0ull;
     // pull gathers through the CSC sources renumbered by out-degree class (hot frontier words share
     // cache lines), with a renumbered copy of each frontier; on one graph with the host-driven loop
-    const bool renum = one_graph && !g->use_cuda_graph && g->E > 0 && want_relabel(g);
+    const bool renum = one_graph && !g->use_cuda_graph && g->batch_launch != 1 && g->E > 0 && want_relabel(g);
     if (renum) {
         EG_TRY(setup_relabel(g));
         EG_TRY(b.wr0.reserve(8 * V + 8));
@@ -954,7 +1136,77 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         }
         return EG_OK;
     };
-    if (g->use_cuda_graph) {
+    if (g->batch_launch == 1) {
+        // the whole traversal in one persistent cooperative launch
+        EG_TRY(enqueue_init());
+        EG_TRY(b.persist.reserve(sizeof(PersistWords)));
+        PersistWords* pw = b.persist.as<PersistWords>();
+        EG_CUDA(cudaMemsetAsync(pw, 0, sizeof(PersistWords), g->stream));
+        const int P = g->partitions;
+        const uint64_t max_tiles = ((V + 1) * (uint64_t)P + kScanTile - 1) / kScanTile + 2;
+        EG_TRY(g->scan.desc.reserve(max_tiles * sizeof(uint64_t)));
+        const size_t smem = 6 * ((size_t)kPullChunk + P + 3);
+        EG_CUDA(cudaFuncSetAttribute(k_msbfs_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_msbfs_persistent, 256, smem));
+        if (per_sm < 1) {
+            set_error("eg_msbfs: the persistent traversal does not fit an SM");
+            return EG_ERR_UNSUPPORTED;
+        }
+        MsPersistArgs pa;
+        pa.V = V;
+        pa.nwords = nwords;
+        pa.P = P;
+        pa.csr_off = g->csr_off.as<uint64_t>();
+        pa.csr_adj = g->csr_adj.as<uint32_t>();
+        pa.gather_adj = gather_adj;
+        pa.cidx = g->cidx.as<uint64_t>();
+        pa.cvert = g->cvert.as<uint32_t>();
+        pa.nitems = g->ncompressed - 1;
+        pa.pull_chunk_item = s.pull_chunk_item.as<uint32_t>();
+        pa.E = g->E;
+        pa.deg = deg;
+        pa.visit = visit;
+        pa.word0 = word[0];
+        pa.word1 = word[1];
+        pa.bm0 = bm[0];
+        pa.bm1 = bm[1];
+        pa.q0 = queue[0];
+        pa.q1 = queue[1];
+        pa.alive_all = alive + 2;
+        pa.lev = lev;
+        pa.ms_seg = b.ms_seg.as<unsigned long long>();
+        pa.desc = g->scan.desc.as<uint64_t>();
+        pa.ipref = s.qdeg.as<uint64_t>();
+        pa.push_chunk_item = s.chunk_item.as<uint32_t>();
+        pa.init_n = d_nq;
+        pa.init_act = d_act;
+        pa.dense_min = g->E / (uint64_t)g->dense_div;
+        pa.early_after_first = one_graph ? 1 : 0;
+        pa.built_csr = g->built_csr ? 1 : 0;
+        pa.w = pw;
+        void* kargs[] = {&pa};
+        {
+            Timed t(&g->prof, g->stream, "msbfs_persistent");
+            EG_CUDA(cudaLaunchCooperativeKernel((const void*)k_msbfs_persistent, dim3((unsigned)g->num_sms * per_sm),
+                                                dim3(256), kargs, smem, g->stream));
+            EG_CHECK_LAUNCH("k_msbfs_persistent");
+        }
+        PersistWords hw;
+        EG_CUDA(cudaMemcpyAsync(&hw, pw, sizeof(PersistWords), cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaStreamSynchronize(g->stream));
+        if (hw.err) {
+            set_error("eg_msbfs: a bounded wait of the persistent traversal gave up");
+            return EG_ERR_TIMEOUT;
+        }
+        if (hw.levels >= 254 && hw.cnt[253] > 0) {
+            set_error("eg_msbfs: more than 254 levels");
+            return EG_ERR_UNSUPPORTED;
+        }
+        sweeps = (int)hw.levels;
+        pushes = (int)hw.pushes;
+        lvl = hw.levels;
+    } else if (g->use_cuda_graph) {
         // init + kGraphLevels levels replayed as one CUDA graph, each level choosing push or pull
         // on the device (k_cap_decide); levels after an empty frontier do nothing
         const bool key_ok = b.graph_exec && b.graph_V == V && b.graph_lev == (lev != nullptr) &&

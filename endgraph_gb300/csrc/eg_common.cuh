@@ -183,6 +183,7 @@ struct eg_graph {
     int bfs_direction = 0;  // 0: Gemini threshold switch, 1: push only, 2: pull only
     int dense_div = 20;     // sparse iff active_edges < E / dense_div (core/graph.hpp:1491)
     int use_cuda_graph = 0; // batched BFS: replay the level loop as one captured CUDA graph
+    int batch_launch = 0;   // batched BFS: 1 runs every level inside one persistent launch
     int pull_blocks_per_sm = 0;  // pull-sweep grid; 0 = occupancy limit
     int batch_width = 64;        // roots per bit-parallel pass (eg_bfs_many)
     int pr_relabel = -1;         // PageRank gathers through renumbered sources: 1 on, 0 off, -1 automatic

@@ -197,9 +197,14 @@ enum {
                                       the values most gathered share cache lines; the same values
                                       are summed per destination.  1 on, 0 off, -1 automatic (on
                                       for V > 2^22; the default) */
-    EG_OPT_MAX_ITERATIONS = 8      /* T of the CPBT page weight for the next build (the public
+    EG_OPT_MAX_ITERATIONS = 8,     /* T of the CPBT page weight for the next build (the public
                                       max_iterations field of Graph, core/graph.hpp:733-738);
                                       eg_config.max_iterations sets it at creation */
+    EG_OPT_BATCH_LAUNCH = 9        /* batched BFS (eg_msbfs, eg_msbfs_graphs): 1 runs the whole
+                                      traversal in one persistent cooperative launch (every level,
+                                      with the push/pull switch and the queue lengths on the
+                                      device; bounded grid barriers); 0 the host-driven loop or,
+                                      with EG_OPT_CUDA_GRAPH, the captured one */
 };
 int eg_set_option(eg_graph* g, int option, int64_t value);
 

@@ -71,22 +71,15 @@ __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
     return v;
 }
 
+// The scan's work for one CTA of 256 threads: tiles by ticket until they run out (callable from
+// a persistent kernel, whose CTAs are all resident, as well as from k_scan)
 template <class Load, class Epi>
-__global__ void __launch_bounds__(kScanThreads) k_scan(Load load, Epi epi, uint64_t n, uint64_t* desc,
-                                                        uint32_t* ticket, int* err, uint64_t* total_out,
-                                                        uint32_t spin_cap, const uint32_t* n_dev = nullptr,
-                                                        uint32_t n_mult = 1) {
+__device__ __forceinline__ void scan_tiles(Load load, Epi epi, uint64_t n, uint64_t* desc, uint32_t* ticket, int* err,
+                                           uint64_t* total_out, uint32_t spin_cap) {
     __shared__ uint32_t s_vals[kScanTile + kScanTile / 32];
     __shared__ uint64_t s_warp[kScanThreads / 32];
     __shared__ uint64_t s_prefix;
     __shared__ uint32_t s_tile;
-    // n_dev: the item count is read on the device (at most n), for launches whose grid is sized for
-    // the largest count (a captured graph); the tiles past it leave at once.  No tile waits on a
-    // later tile, and tile 0 always runs, so the total is written even for zero items.
-    if (n_dev) {
-        const uint64_t nd = (uint64_t)__ldcg(n_dev) * n_mult;
-        n = nd < n ? nd : n;
-    }
     // a CTA takes tiles by ticket until they run out, so a grid smaller than the tile count works
     // too (tiles are taken in order by running CTAs, so every wait is on a running tile)
     while (true) {
@@ -179,6 +172,21 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Load load, Epi epi, uint6
         if (base + kScanTile >= n) return;  // the last tile: nothing left to take
         __syncthreads();                    // s_tile, s_vals and s_prefix are reused by the next tile
     }
+}
+
+template <class Load, class Epi>
+__global__ void __launch_bounds__(kScanThreads) k_scan(Load load, Epi epi, uint64_t n, uint64_t* desc,
+                                                        uint32_t* ticket, int* err, uint64_t* total_out,
+                                                        uint32_t spin_cap, const uint32_t* n_dev = nullptr,
+                                                        uint32_t n_mult = 1) {
+    // n_dev: the item count is read on the device (at most n), for launches whose grid is sized for
+    // the largest count (a captured graph); the tiles past it leave at once.  No tile waits on a
+    // later tile, and tile 0 always runs, so the total is written even for zero items.
+    if (n_dev) {
+        const uint64_t nd = (uint64_t)__ldcg(n_dev) * n_mult;
+        n = nd < n ? nd : n;
+    }
+    scan_tiles(load, epi, n, desc, ticket, err, total_out, spin_cap);
 }
 
 
@@ -352,18 +360,27 @@ __global__ void __launch_bounds__(kPullThreads, 5) k_pull(Op op, const uint32_t*
 // memory (6 bytes per item, so eight CTAs fit an SM); a segment closed inside a thread's 16 edges
 // is applied at once, and the open segments at the ends of threads are merged along the warp
 // first.  No second barrier, so CTAs retire as soon as their own chunk is done.
+// The chunks of one CTA (chunk blockIdx.x, then every gridDim.x-th), staging in s_raw
+// ticket (optional): chunks are taken from this counter instead of by stride, which balances
+// uneven chunks when a persistent grid runs the sweep
 template <class Op>
-__global__ void __launch_bounds__(kPullThreads) k_pull_direct(Op op, const uint32_t* __restrict__ adj,
-                                                               const uint64_t* __restrict__ cidx,
-                                                               const uint32_t* __restrict__ cvert,
-                                                               const uint32_t* __restrict__ chunk_item, uint64_t E,
-                                                               uint64_t nitems, uint32_t V) {
+__device__ __forceinline__ void pull_direct_chunks(const Op& op, const uint32_t* __restrict__ adj,
+                                                   const uint64_t* __restrict__ cidx, const uint32_t* __restrict__ cvert,
+                                                   const uint32_t* __restrict__ chunk_item, uint64_t E, uint64_t nitems,
+                                                   uint32_t V, unsigned char* s_raw, uint32_t* ticket = nullptr) {
     using Acc = typename Op::Acc;
-    if (op.stopped()) return;
-    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ uint32_t s_chunk;
     // one chunk per CTA when launched with a CTA per chunk; a smaller (persistent) grid strides
     const uint64_t nchunks = (E + kPullChunk - 1) / kPullChunk;
-    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    auto take = [&](uint64_t dflt) -> uint64_t {
+        if (!ticket) return dflt;
+        if (threadIdx.x == 0) s_chunk = atomicAdd(ticket, 1u);
+        __syncthreads();
+        const uint64_t t = s_chunk;
+        __syncthreads();
+        return t;
+    };
+    for (uint64_t c = take(blockIdx.x); c < nchunks; c = take(c + gridDim.x)) {
         const uint64_t e0 = c * kPullChunk;
         const uint64_t e1 = e0 + kPullChunk < E ? e0 + kPullChunk : E;
         const uint32_t i0 = chunk_item[c];
@@ -452,8 +469,19 @@ __global__ void __launch_bounds__(kPullThreads) k_pull_direct(Op op, const uint3
         const int knext = __shfl_down_sync(0xffffffffu, fin_key, 1);
         if (fin_key != 0x7fffffff && (lane == 31 || knext != fin_key) && fin != op.identity())
             op.finish_direct(s_v[fin_key], fin);
-        if (c + gridDim.x < nchunks) __syncthreads();  // the next chunk reuses the staged entries
+        if (ticket || c + gridDim.x < nchunks) __syncthreads();  // the next chunk reuses the staged entries
     }
+}
+
+template <class Op>
+__global__ void __launch_bounds__(kPullThreads) k_pull_direct(Op op, const uint32_t* __restrict__ adj,
+                                                               const uint64_t* __restrict__ cidx,
+                                                               const uint32_t* __restrict__ cvert,
+                                                               const uint32_t* __restrict__ chunk_item, uint64_t E,
+                                                               uint64_t nitems, uint32_t V) {
+    if (op.stopped()) return;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    pull_direct_chunks(op, adj, cidx, cvert, chunk_item, E, nitems, V, s_raw);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -565,8 +593,9 @@ struct push_value<Op, std::void_t<typename Op::Value>> {
     using type = typename Op::Value;
 };
 
+// The rank-balanced expansion for one CTA of kPushThreads (chunks blockIdx.x, +gridDim.x, ...)
 template <class Op>
-__global__ void __launch_bounds__(kPushThreads) k_push(Op op, PushArgs a) {
+__device__ __forceinline__ void push_chunks(const Op& op, PushArgs a) {
     using Val = typename push_value<Op>::type;
     constexpr bool kReduce = !std::is_void<Val>::value;
     std::conditional_t<kReduce, Val, int> acc{};
@@ -666,6 +695,11 @@ __global__ void __launch_bounds__(kPushThreads) k_push(Op op, PushArgs a) {
     }
 }
 
+template <class Op>
+__global__ void __launch_bounds__(kPushThreads) k_push(Op op, PushArgs a) {
+    push_chunks(op, a);
+}
+
 // scan over frontier items: item length -> exclusive rank, and chunk -> first item
 struct LoadItemLen {
     const uint32_t* q;
@@ -690,8 +724,9 @@ struct EpiItemRank {
 
 // next frontier bitmap -> vertex queue, its length and the out-edges of the queued vertices;
 // one warp per 32 words
-static __global__ void k_bm_compact(const unsigned long long* __restrict__ bm, uint64_t nwords, uint32_t* q, uint32_t* nq,
-                             unsigned long long* act_edges, const uint32_t* __restrict__ deg) {
+__device__ __forceinline__ void bm_compact_words(const unsigned long long* __restrict__ bm, uint64_t nwords, uint32_t* q,
+                                                 uint32_t* nq, unsigned long long* act_edges,
+                                                 const uint32_t* __restrict__ deg) {
     const int lane = threadIdx.x & 31;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < nwords; base += stride) {
@@ -720,6 +755,11 @@ static __global__ void k_bm_compact(const unsigned long long* __restrict__ bm, u
         for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
         if (lane == 0 && act_edges && d) atomicAdd(act_edges, d);
     }
+}
+
+static __global__ void k_bm_compact(const unsigned long long* __restrict__ bm, uint64_t nwords, uint32_t* q, uint32_t* nq,
+                                    unsigned long long* act_edges, const uint32_t* __restrict__ deg) {
+    bm_compact_words(bm, nwords, q, nq, act_edges, deg);
 }
 
 

@@ -58,10 +58,10 @@ def test_msbfs_renumbered_gathers(eg_lib, direction_div):
             assert run["push"] == 0
 
 
-@pytest.mark.parametrize("cuda_graph", [0, 1])
-def test_msbfs_cuda_graph_mode(eg_lib, cuda_graph):
-    """The captured 32-level loop (each level choosing push or pull on the device) gives the same
-    levels as the host-driven loop, and takes both directions as the host loop does."""
+@pytest.mark.parametrize("cuda_graph,persistent", [(0, 0), (1, 0), (0, 1)])
+def test_msbfs_cuda_graph_mode(eg_lib, cuda_graph, persistent):
+    """The captured level loop and the persistent launch (each level choosing push or pull on the
+    device) give the same levels as the host-driven loop, and take both directions as it does."""
     import endgraph_gb300 as eg
     V, E = 1 << 13, 1 << 16
     src, dst, _ = rmat_graph(V, E, 97)
@@ -70,6 +70,7 @@ def test_msbfs_cuda_graph_mode(eg_lib, cuda_graph):
     with eg.Graph() as g:
         g.load_directed(eg.pack_edges(src, dst), V)
         g.set_option(eg.EG_OPT_CUDA_GRAPH, cuda_graph)
+        g.set_option(eg.EG_OPT_BATCH_LAUNCH, persistent)
         for rep in range(2):  # the second call replays the cached graph
             levels, _ = g.msbfs(roots[rep * 8:] if rep else roots)
             use = roots[rep * 8:] if rep else roots
@@ -117,8 +118,8 @@ def _graph_batch(G, seed, weighted=False):
     return Vs, eoff, parts, src, dst, w
 
 
-@pytest.mark.parametrize("cuda_graph", [0, 1])
-def test_graph_batch_msbfs(eg_lib, cuda_graph):
+@pytest.mark.parametrize("cuda_graph,persistent", [(0, 0), (1, 0), (0, 1)])
+def test_graph_batch_msbfs(eg_lib, cuda_graph, persistent):
     """Many small graphs preprocessed together; 64 roots per graph; every graph matches the oracle."""
     import endgraph_gb300 as eg
     G = 40
@@ -128,6 +129,7 @@ def test_graph_batch_msbfs(eg_lib, cuda_graph):
     with eg.Graph() as g:
         g.load_graph_batch(eg.pack_edges(src, dst), eoff, Vs)
         g.set_option(eg.EG_OPT_CUDA_GRAPH, cuda_graph)
+        g.set_option(eg.EG_OPT_BATCH_LAUNCH, persistent)
         voff, eo = g.graph_batch()
         assert np.array_equal(eo, eoff) and voff[-1] == Vs.sum()
         levels, _ = g.msbfs_graphs(roots, 64)

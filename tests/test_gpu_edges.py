@@ -85,8 +85,9 @@ def test_deep_path(eg_lib):
         g.load_directed(eg.pack_edges(src, dst), n)
         lv, _ = g.bfs(0)
         assert np.array_equal(lv, np.arange(n))
-        for cg in (0, 1):
+        for cg, pers in ((0, 0), (1, 0), (0, 1)):
             g.set_option(eg.EG_OPT_CUDA_GRAPH, cg)
+            g.set_option(eg.EG_OPT_BATCH_LAUNCH, pers)
             levels, edges = g.msbfs(np.array([0, 50], np.uint32))
             assert np.array_equal(levels[0], np.arange(n, dtype=np.uint8))
             assert np.array_equal(levels[1][50:], np.arange(n - 50, dtype=np.uint8))
@@ -96,6 +97,9 @@ def test_deep_path(eg_lib):
     src = np.arange(m - 1, dtype=np.uint32)
     with eg.Graph() as g:
         g.load_directed(eg.pack_edges(src, src + 1), m)
+        with pytest.raises(eg.EndGraphError):
+            g.msbfs(np.array([0], np.uint32))
+        g.set_option(eg.EG_OPT_BATCH_LAUNCH, 1)
         with pytest.raises(eg.EndGraphError):
             g.msbfs(np.array([0], np.uint32))
 
