@@ -25,7 +25,7 @@ LIB_PATH = _build.LIB
 EG_HOST, EG_DEVICE = 0, 1
 EG_OPT_BFS_DIRECTION, EG_OPT_DENSE_DIVISOR, EG_OPT_CUDA_GRAPH = 1, 2, 3
 EG_OPT_PULL_BLOCKS_PER_SM, EG_OPT_BATCH_WIDTH, EG_OPT_SSSP_DELTA, EG_OPT_PR_RELABEL = 4, 5, 6, 7
-EG_OPT_MAX_ITERATIONS, EG_OPT_BATCH_LAUNCH = 8, 9
+EG_OPT_MAX_ITERATIONS, EG_OPT_BATCH_LAUNCH, EG_OPT_BATCH_DIVISOR = 8, 9, 10
 STATUS = {0: "EG_OK", 1: "EG_ERR_INVALID", 2: "EG_ERR_CUDA", 3: "EG_ERR_NOMEM", 4: "EG_ERR_STATE",
           5: "EG_ERR_TIMEOUT", 6: "EG_ERR_HOST_CALLBACK", 7: "EG_ERR_UNSUPPORTED"}
 
@@ -50,11 +50,11 @@ class Info(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("bfs_direction", ctypes.c_int32), ("dense_divisor", ctypes.c_int32),
                 ("pull_blocks_per_sm", ctypes.c_int32), ("cuda_graph", ctypes.c_int32), ("batch_width", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("bfs_ms", ctypes.c_double), ("pull_sweep_ms", ctypes.c_double),
+                ("batch_divisor", ctypes.c_int32), ("bfs_ms", ctypes.c_double), ("pull_sweep_ms", ctypes.c_double),
                 ("msbfs_ms_per_root", ctypes.c_double)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class KernelStat(ctypes.Structure):

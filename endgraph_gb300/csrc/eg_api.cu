@@ -853,6 +853,10 @@ int eg_set_option(eg_graph* g, int option, int64_t value) {
             if (value < 0 || value > 1) break;
             g->batch_launch = (int)value;
             return EG_OK;
+        case EG_OPT_BATCH_DIVISOR:
+            if (value < 0 || value > (1 << 30)) break;
+            g->batch_div = (int)value;
+            return EG_OK;
         case EG_OPT_MAX_ITERATIONS:
             if (value < 0 || value > INT32_MAX) break;
             g->max_iterations = (int)value;

@@ -686,6 +686,7 @@ struct BatchState {
     bool graph_lev = false;
     uint32_t graph_entries = 0;
     int graph_nbits = 0;
+    int graph_div = 0;  // the switch's divisor the captured levels compare with
     ~BatchState() {
         if (graph_exec) cudaGraphExecDestroy((cudaGraphExec_t)graph_exec);
     }
@@ -1115,7 +1116,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
                 return EG_ERR_UNSUPPORTED;
             }
             // the Gemini switch on the union frontier; EG_OPT_BFS_DIRECTION concerns single-root BFS
-            const bool dense = !g->built_csr || act >= g->E / (uint64_t)g->dense_div;
+            const bool dense = !g->built_csr || act >= g->E / (uint64_t)batch_divisor(g);
             uint32_t nout = 0;
             // a bitmap test before each gather pays only while the frontier is a small part of V
             EG_TRY(enqueue_level(lvl, n, dense, n * 16 < V, d_nq, nullptr, &nout, &act, one_graph && dense_levels > 0,
@@ -1181,7 +1182,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         pa.push_chunk_item = s.chunk_item.as<uint32_t>();
         pa.init_n = d_nq;
         pa.init_act = d_act;
-        pa.dense_min = g->E / (uint64_t)g->dense_div;
+        pa.dense_min = g->E / (uint64_t)batch_divisor(g);
         pa.early_after_first = one_graph ? 1 : 0;
         pa.built_csr = g->built_csr ? 1 : 0;
         pa.w = pw;
@@ -1210,7 +1211,8 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         // init + kGraphLevels levels replayed as one CUDA graph, each level choosing push or pull
         // on the device (k_cap_decide); levels after an empty frontier do nothing
         const bool key_ok = b.graph_exec && b.graph_V == V && b.graph_lev == (lev != nullptr) &&
-                            b.graph_entries >= n_entries && b.graph_nbits == nbits;
+                            b.graph_entries >= n_entries && b.graph_nbits == nbits &&
+                            b.graph_div == batch_divisor(g);
         if (!key_ok) {
             if (b.graph_exec) cudaGraphExecDestroy((cudaGraphExec_t)b.graph_exec);
             b.graph_exec = nullptr;
@@ -1230,7 +1232,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
             };
             ok(cudaMemsetAsync(cs, 0, sizeof(CapState), g->stream));
             ok(cudaMemsetAsync(word[1], 0, 8 * V, g->stream));
-            const unsigned long long dense_min = g->E / (uint64_t)g->dense_div;
+            const unsigned long long dense_min = g->E / (uint64_t)batch_divisor(g);
             for (uint32_t L = 0; st == EG_OK && L < (uint32_t)kGraphLevels; ++L) {
                 const int c = L & 1, x = c ^ 1;
                 const uint32_t* n_cur = L == 0 ? d_nq : cnt + L - 1;
@@ -1315,6 +1317,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
             b.graph_lev = lev != nullptr;
             b.graph_entries = n_entries;
             b.graph_nbits = nbits;
+            b.graph_div = batch_divisor(g);
         }
         {
             Timed t(&g->prof, g->stream, "msbfs_graph");

@@ -184,6 +184,7 @@ struct eg_graph {
     int dense_div = 20;     // sparse iff active_edges < E / dense_div (core/graph.hpp:1491)
     int use_cuda_graph = 0; // batched BFS: replay the level loop as one captured CUDA graph
     int batch_launch = 0;   // batched BFS: 1 runs every level inside one persistent launch
+    int batch_div = 0;      // batched BFS switch divisor; 0: the same as dense_div
     int pull_blocks_per_sm = 0;  // pull-sweep grid; 0 = occupancy limit
     int batch_width = 64;        // roots per bit-parallel pass (eg_bfs_many)
     int pr_relabel = -1;         // PageRank gathers through renumbered sources: 1 on, 0 off, -1 automatic
@@ -249,6 +250,9 @@ int load_graph_batch(eg_graph* g, const void* edges, int rec, const uint64_t* eo
 int run_msbfs_graphs(eg_graph* g, const uint32_t* roots, int nper, uint8_t* levels, int where, uint64_t* edges);
 int run_sssp_graphs(eg_graph* g, const uint32_t* sources, int nper, float* dist, int where);
 int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E);
+
+// the push/pull switch of the batched traversals: sparse iff the frontier's out-edges < E / this
+inline int batch_divisor(const eg_graph* g) { return g->batch_div > 0 ? g->batch_div : g->dense_div; }
 
 // device helpers
 __device__ __forceinline__ uint32_t part_of(const uint32_t* __restrict__ off, int P, uint32_t v) {

@@ -4,7 +4,8 @@
 //   dense divisor     process_edges runs sparse iff active out-edges < E / divisor (BFS), or
 //                     push-only as the reference's use_root mode
 //   pull CTAs per SM  grid of the chunked pull sweep (1, 2, 3, 4, or the occupancy limit)
-//   CUDA graph        batched BFS level loop replayed as a captured graph or driven from the host
+//   CUDA graph        batched BFS level loop replayed as a captured graph or driven from the host,
+//                     with the batched traversal's own switch divisor
 //   batch width       roots per bit-parallel pass in eg_bfs_many (16, 32 or 64)
 // Each candidate is timed as the median of five synchronous runs over up to 16 sample roots; the
 // first candidate of each setting is the current one (the reference's E/20 for the switch), and a
@@ -131,24 +132,31 @@ int eg_autotune(eg_graph* g, const uint32_t* sample_roots, int nroots, eg_tuning
     out->pull_blocks_per_sm = best_blocks;
     out->pull_sweep_ms = best / 2;
 
-    // 3. captured level loop for batched BFS
+    // 3. batched BFS: its own switch divisor, and the captured level loop or the host-driven one
     best = 1e30;
-    int best_graph = 0;
+    int best_graph = 0, best_bdiv = 20;
+    const int bdivs[] = {20, 10, 40, 5};
     for (int cg = 0; cg <= 1; ++cg) {
-        g->use_cuda_graph = cg;
-        EG_TRY(run_msbfs(g, r64.data(), 64, nullptr, EG_HOST, nullptr));  // capture outside the timing
-        double ms = 0;
-        EG_TRY(time_median([&]() { return run_msbfs(g, r64.data(), 64, nullptr, EG_HOST, nullptr); }, &ms));
-        if (ms < best * kTuneMargin) {
-            best = ms;
-            best_graph = cg;
+        for (int d : bdivs) {
+            g->use_cuda_graph = cg;
+            g->batch_div = d;
+            EG_TRY(run_msbfs(g, r64.data(), 64, nullptr, EG_HOST, nullptr));  // capture outside the timing
+            double ms = 0;
+            EG_TRY(time_median([&]() { return run_msbfs(g, r64.data(), 64, nullptr, EG_HOST, nullptr); }, &ms));
+            if (ms < best * kTuneMargin) {
+                best = ms;
+                best_graph = cg;
+                best_bdiv = d;
+            }
         }
     }
     g->use_cuda_graph = best_graph;
+    g->batch_div = best_bdiv;
     out->cuda_graph = best_graph;
+    out->batch_divisor = best_bdiv;
 
     // 4. roots per bit-parallel pass
-    const int widths[] = {16, 32, 64};
+    const int widths[] = {64, 32, 16};  // the default first
     best = 1e30;
     int best_w = 64;
     for (int w : widths) {

@@ -200,11 +200,13 @@ enum {
     EG_OPT_MAX_ITERATIONS = 8,     /* T of the CPBT page weight for the next build (the public
                                       max_iterations field of Graph, core/graph.hpp:733-738);
                                       eg_config.max_iterations sets it at creation */
-    EG_OPT_BATCH_LAUNCH = 9        /* batched BFS (eg_msbfs, eg_msbfs_graphs): 1 runs the whole
+    EG_OPT_BATCH_LAUNCH = 9,       /* batched BFS (eg_msbfs, eg_msbfs_graphs): 1 runs the whole
                                       traversal in one persistent cooperative launch (every level,
                                       with the push/pull switch and the queue lengths on the
                                       device; bounded grid barriers); 0 the host-driven loop or,
                                       with EG_OPT_CUDA_GRAPH, the captured one */
+    EG_OPT_BATCH_DIVISOR = 10      /* the switch of the batched BFS (push iff the union frontier's
+                                      out-edges < E / divisor); 0 (the default): EG_OPT_DENSE_DIVISOR */
 };
 int eg_set_option(eg_graph* g, int option, int64_t value);
 
@@ -259,7 +261,7 @@ typedef struct eg_tuning {
     int32_t pull_blocks_per_sm; /* EG_OPT_PULL_BLOCKS_PER_SM chosen (0: occupancy limit) */
     int32_t cuda_graph;         /* EG_OPT_CUDA_GRAPH chosen */
     int32_t batch_width;        /* EG_OPT_BATCH_WIDTH chosen */
-    int32_t reserved;
+    int32_t batch_divisor;      /* EG_OPT_BATCH_DIVISOR chosen */
     double bfs_ms;              /* best single-root BFS time */
     double pull_sweep_ms;       /* best pull-sweep time (one PageRank iteration) */
     double msbfs_ms_per_root;   /* best batched BFS time per root */

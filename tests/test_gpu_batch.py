@@ -92,6 +92,7 @@ def test_autotune_keeps_results(eg_lib):
         g.load_directed(eg.pack_edges(src, dst), V)
         t = g.autotune(roots[:8])
         assert t["batch_width"] in (16, 32, 64) and t["cuda_graph"] in (0, 1)
+        assert t["batch_divisor"] in (5, 10, 20, 40)
         assert t["bfs_ms"] > 0 and t["pull_sweep_ms"] > 0
         lv, _ = g.bfs(int(roots[0]))
         assert np.array_equal(lv, oracle.bfs_levels(csr["off"][0], csr["adj"], V, int(roots[0])))
