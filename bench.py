@@ -258,12 +258,13 @@ ALG_BYTES = {  # algorithmic bytes per launch (E edges, V vertices, nc compresse
 }
 
 
-TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "dram_traffic_rmat-s25-ef16.md")
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "pr_pull_traffic_rmat-s25-ef16.md")
 
 
 def profiled_traffic(args):
     """DRAM bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum) of the bench's
-    kernels, from the committed summary of a capture of this workload: rows
+    dominant kernel, from the committed summary of a one-kernel, one-pass capture of this workload:
+    rows
     `| `bench name` | kernel | launches | read GB | write GB | bytes per launch |`."""
     if args.scale != 25 or args.edge_factor != 16 or not os.path.exists(TRAFFIC_PROFILE):
         return {}
