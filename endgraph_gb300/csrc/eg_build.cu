@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_hist(const uint8_t* _
     for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) cnt[(uint64_t)i * nblk + blockIdx.x] = s_h[i];
 }
 
-// in-place exclusive scan of s[0..n) by the whole block; returns the total
+// in-place exclusive scan of s[0..n) by the whole block; returns the total.  s_warp: 33 words
 __device__ uint32_t block_exclusive_scan(uint32_t* s, uint32_t n, uint32_t* s_warp) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
@@ -362,13 +362,20 @@ __device__ uint32_t block_exclusive_scan(uint32_t* s, uint32_t n, uint32_t* s_wa
     }
     if (lane == 31) s_warp[warp] = inc;
     __syncthreads();
-    uint32_t wb = 0, total = 0;
-    for (int w = 0; w < nw; ++w) {
-        uint32_t x = s_warp[w];
-        if (w < warp) wb += x;
-        total += x;
+    if (warp == 0) {  // exclusive scan of the warp totals, the block total in s_warp[32]
+        const uint32_t x = lane < nw ? s_warp[lane] : 0u;
+        uint32_t y = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t z = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= o) y += z;
+        }
+        if (lane < nw) s_warp[lane] = y - x;
+        if (lane == 31) s_warp[32] = y;
     }
-    uint32_t run = wb + inc - tsum;
+    __syncthreads();
+    const uint32_t total = s_warp[32];
+    uint32_t run = s_warp[warp] + inc - tsum;
     for (uint32_t j = 0; j < per; ++j) {
         if (b0 + j < n) {
             uint32_t c = s[b0 + j];
@@ -402,7 +409,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_
     unsigned long long* s_base = reinterpret_cast<unsigned long long*>(s_raw);  // [2][nb]
     uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_base + 2 * nb);            // [nb]
     uint32_t* s_stage = reinterpret_cast<uint32_t*>(s_raw + align16(20ull * nb));  // [tile][W]
-    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_warp[33];
     for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_base[i] = excl[(uint64_t)i * nblk + blockIdx.x];
     const uint64_t e0 = blockIdx.x * chunk;
     const uint64_t e1 = e0 + chunk < E ? e0 + chunk : E;
@@ -417,9 +424,15 @@ __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_
             const uint64_t e = t0 + (uint64_t)j * blockDim.x + threadIdx.x;
             valid[j] = e < e1;
             if (valid[j]) {
-                const uint32_t* r = reinterpret_cast<const uint32_t*>(edges + e * REC);
+                if (W == 2) {
+                    const uint2 x = __ldcs(reinterpret_cast<const uint2*>(edges) + e);
+                    rec[j][0] = x.x;
+                    rec[j][1] = x.y;
+                } else {
+                    const uint32_t* r = reinterpret_cast<const uint32_t*>(edges + e * REC);
 #pragma unroll
-                for (int w = 0; w < W; ++w) rec[j][w] = __ldcs(r + w);
+                    for (int w = 0; w < W; ++w) rec[j][w] = __ldcs(r + w);
+                }
                 if (kCheck) valid[j] = rec[j][0] < V && rec[j][1] < V;  // pass A skipped it too
             }
         }
@@ -550,7 +563,7 @@ __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* _
     unsigned long long keep;
     asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(keep));
     extern __shared__ uint32_t s_cnt[];  // LB counters
-    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_b;
     __shared__ uint64_t s_lo[kMaxParts], s_hi[kMaxParts];
     __shared__ uint64_t s_r0, s_r1;
