@@ -69,15 +69,18 @@ static int launch_pull(eg_graph* g, const Op& op, const char* name, const uint32
     // a chunk holds at most one item per edge plus the zero-length sentinels of empty partitions
     const int cap = (int)kPullChunk + g->partitions + 2;
     const size_t smem = pull_acc_offset(cap) + sizeof(typename Op::Acc) * cap + (Op::kFilter ? cap : 0);
-    EG_CUDA(cudaFuncSetAttribute(k_pull<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // gathers through renumbered sources mostly hit L2: six CTAs per SM (2.40 against 2.49 ms per
+    // PageRank sweep at 2^25 / 2^29); in vertex order they need the larger L1 of five (3.13 / 3.61)
+    auto kern = adj ? k_pull<Op, 6> : k_pull<Op, 5>;
+    EG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pull<Op>, kPullThreads, smem));
+    EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPullThreads, smem));
     if (g->pull_blocks_per_sm > 0) per_sm = std::min(per_sm, g->pull_blocks_per_sm);
     unsigned grid = (unsigned)std::min<uint64_t>(s.pull_nchunks, (uint64_t)g->num_sms * (uint64_t)std::max(per_sm, 1));
     Timed t(&g->prof, g->stream, name);
-    k_pull<Op><<<grid, kPullThreads, smem, g->stream>>>(op, adj ? adj : g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(),
-                                                        g->cvert.as<uint32_t>(), s.pull_chunk_item.as<uint32_t>(), g->E,
-                                                        nitems, s.pull_nchunks, g->V, cap);
+    kern<<<grid, kPullThreads, smem, g->stream>>>(op, adj ? adj : g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(),
+                                                  g->cvert.as<uint32_t>(), s.pull_chunk_item.as<uint32_t>(), g->E,
+                                                  nitems, s.pull_nchunks, g->V, cap);
     EG_CHECK_LAUNCH(name);
     return EG_OK;
 }

@@ -224,8 +224,10 @@ __host__ __device__ constexpr size_t pull_acc_offset(int cap) { return align16(s
 // Generic segmented pull over compressed CSC entries.  Op provides:
 //   Acc identity(); Acc gather(uint32_t src, uint64_t epos); Acc combine(Acc, Acc);
 //   void smem_add(Acc* slot, Acc v); void finish(uint32_t v, Acc a, bool whole)
-template <class Op>
-__global__ void __launch_bounds__(kPullThreads, 5) k_pull(Op op, const uint32_t* __restrict__ adj,
+// kMinBlocks: CTAs per SM the registers are sized for (5: 48 registers; 6: 40, for gathers that
+// mostly hit L2, which gain more from the sixth CTA than they lose to the smaller L1)
+template <class Op, int kMinBlocks = 5>
+__global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_pull(Op op, const uint32_t* __restrict__ adj,
                                                         const uint64_t* __restrict__ cidx,
                                                         const uint32_t* __restrict__ cvert,
                                                         const uint32_t* __restrict__ chunk_item, uint64_t E,

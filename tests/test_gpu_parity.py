@@ -110,6 +110,44 @@ def test_pagerank_renumbered_gathers(eg_lib, P):
         assert rel_l1(g.pagerank(20, 0.85), ref2) <= 1e-6
 
 
+def _in_degree_graph(indeg, V, seed):
+    """Edges whose destinations 0..len(indeg)-1 have the given in-degrees, from random sources."""
+    rng = np.random.default_rng(seed)
+    dst = np.repeat(np.arange(len(indeg), dtype=np.uint32), indeg)
+    src = rng.integers(0, V, len(dst), dtype=np.uint32)
+    perm = rng.permutation(len(dst))
+    return src[perm], dst[perm]
+
+
+@pytest.mark.parametrize("shape", ["hub", "degree1", "degree16", "degree4096", "tiny", "ragged"])
+def test_pagerank_chunk_shapes(eg_lib, shape):
+    """The one-partition sweep cuts the CSC into 4,096-edge CTA chunks of 16-edge threads: in-lists
+    that span chunks (a 9,000-edge hub), chunks of 4,096 one-edge lists, lists that end exactly on
+    thread and chunk boundaries, fewer edges than one chunk, and a ragged last chunk all match the
+    oracle, with and without renumbered gathers."""
+    import endgraph_gb300 as eg
+    V = 4096
+    rng = np.random.default_rng(5)
+    indeg = {
+        "hub": np.concatenate([[9000], rng.integers(1, 40, 600), [1300], rng.integers(0, 3, 500)]),
+        "degree1": np.ones(4096 * 2 + 100, np.int64)[:V],
+        "degree16": np.full(700, 16),
+        "degree4096": np.full(3, 4096),
+        "tiny": np.array([1, 0, 3, 2]),
+        "ragged": np.concatenate([rng.integers(1, 30, 400), [17]]),
+    }[shape]
+    src, dst = _in_degree_graph(indeg, V, 7)
+    o_out, _ = oracle.degrees(src, dst, V)
+    csc = oracle.build_csc(src, dst, None, V, np.array([0, V], np.uint32))
+    ref = oracle.pagerank(csc["off"][0], csc["adj"], o_out, V, 20, 0.85)
+    with _graph(eg_lib) as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        for relabel in (0, 1):
+            g.set_option(eg.EG_OPT_PR_RELABEL, relabel)
+            err = rel_l1(g.pagerank(20, 0.85), ref)
+            assert err <= 1e-6, (relabel, err)
+
+
 @pytest.mark.parametrize("V,E,seed", CASES)
 @pytest.mark.parametrize("P", [1, 2])
 def test_bfs(eg_lib, V, E, seed, P):
