@@ -418,10 +418,16 @@ def run_graph_batch(args, dev):
         s = torch.cuda.ExternalStream(g.stream, device=dev)
         g.load_graph_batch(rec, eoff, Vs)  # warm (allocations)
         t_b, _ = _timed(s, lambda: g.load_graph_batch(rec, eoff, Vs))  # records -> union -> CPBT + CSR + CSC
-        del rec
-        torch.cuda.empty_cache()
         out["build_ms"] = round(t_b, 3)
         out["build_medges_s"] = round(E / t_b / 1e3, 1)
+        # the same build as one persistent cooperative launch (union ids, passes A-C, bitmap, index)
+        g.set_option(eg.EG_OPT_BUILD_LAUNCH, 1)
+        g.load_graph_batch(rec, eoff, Vs)
+        t_1, _ = _timed(s, lambda: g.load_graph_batch(rec, eoff, Vs))
+        g.set_option(eg.EG_OPT_BUILD_LAUNCH, 0)
+        out["build_one_launch_ms"] = round(t_1, 3)
+        del rec
+        torch.cuda.empty_cache()
         # tune on one root from each of 64 graphs spread over the size range (union ids)
         voff, _ = g.graph_batch()
         pick = np.linspace(0, G - 1, 64).astype(np.int64)

@@ -25,7 +25,7 @@ LIB_PATH = _build.LIB
 EG_HOST, EG_DEVICE = 0, 1
 EG_OPT_BFS_DIRECTION, EG_OPT_DENSE_DIVISOR, EG_OPT_CUDA_GRAPH = 1, 2, 3
 EG_OPT_PULL_BLOCKS_PER_SM, EG_OPT_BATCH_WIDTH, EG_OPT_SSSP_DELTA, EG_OPT_PR_RELABEL = 4, 5, 6, 7
-EG_OPT_MAX_ITERATIONS, EG_OPT_BATCH_LAUNCH, EG_OPT_BATCH_DIVISOR = 8, 9, 10
+EG_OPT_MAX_ITERATIONS, EG_OPT_BATCH_LAUNCH, EG_OPT_BATCH_DIVISOR, EG_OPT_BUILD_LAUNCH = 8, 9, 10, 11
 STATUS = {0: "EG_OK", 1: "EG_ERR_INVALID", 2: "EG_ERR_CUDA", 3: "EG_ERR_NOMEM", 4: "EG_ERR_STATE",
           5: "EG_ERR_TIMEOUT", 6: "EG_ERR_HOST_CALLBACK", 7: "EG_ERR_UNSUPPORTED"}
 

@@ -861,6 +861,10 @@ int eg_set_option(eg_graph* g, int option, int64_t value) {
             if (value < 0 || value > INT32_MAX) break;
             g->max_iterations = (int)value;
             return EG_OK;
+        case EG_OPT_BUILD_LAUNCH:
+            if (value != 0 && value != 1) break;
+            g->build_launch = (int)value;
+            return EG_OK;
         default:
             set_error("eg_set_option: unknown option %d", option);
             return EG_ERR_INVALID;

@@ -819,7 +819,6 @@ __global__ void k_clear_front_dev(const uint32_t* __restrict__ q, const uint32_t
 // that could not keep all its CTAs resident is refused by the cooperative launch, and every
 // barrier wait is bounded: on exhaustion the error flag is raised and the kernel returns.
 constexpr int kMaxLevels = 256;
-constexpr uint32_t kBarrierSpinCap = 1u << 22;
 
 struct PersistWords {
     uint32_t cnt[kMaxLevels];          // queue length produced by level L
@@ -867,33 +866,7 @@ struct MsPersistArgs {
 
 // bounded grid barrier (all CTAs resident): false when a wait ran out
 __device__ __forceinline__ bool grid_barrier(PersistWords* w) {
-    __syncthreads();
-    __shared__ int s_ok;
-    if (threadIdx.x == 0) {
-        const unsigned nblocks = gridDim.x;
-        const unsigned gen = *(volatile unsigned*)&w->bar_gen;
-        __threadfence();
-        int ok = 1;
-        if (atomicAdd(&w->bar_count, 1u) == nblocks - 1) {
-            atomicExch(&w->bar_count, 0u);
-            __threadfence();
-            atomicAdd(&w->bar_gen, 1u);
-        } else {
-            uint32_t spins = 0;
-            while (*(volatile unsigned*)&w->bar_gen == gen) {
-                if (++spins > kBarrierSpinCap || *(volatile int*)&w->err) {
-                    atomicExch(&w->err, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
+    return grid_sync_bounded(&w->bar_count, &w->bar_gen, &w->err);
 }
 
 __global__ void __launch_bounds__(256, 4) k_msbfs_persistent(MsPersistArgs a) {
@@ -1930,6 +1903,12 @@ int load_graph_batch(eg_graph* g, const void* edges, int rec, const uint64_t* eo
     EG_TRY(g->tmp64.reserve(8 * (G + 1)));
     EG_CUDA(cudaMemcpyAsync(g->d_batch_voff.ptr, voff.data(), 8 * (G + 1), cudaMemcpyHostToDevice, g->stream));
     EG_CUDA(cudaMemcpyAsync(g->tmp64.ptr, eo.data(), 8 * (G + 1), cudaMemcpyHostToDevice, g->stream));
+    if (g->build_launch && persistent_build_fits(g)) {  // ids moved to the union inside the one launch
+        EG_TRY(build_persistent(g, g->tmp64.as<uint64_t>(), g->d_batch_voff.as<uint64_t>(), (uint32_t)G));
+        g->batch_voff = voff;
+        g->batch_eoff = eo;
+        return EG_OK;
+    }
     EG_CUDA(cudaMemsetAsync(g->err.as<int>() + 1, 0, sizeof(int), g->stream));
     if (E) {
         Timed t(&g->prof, g->stream, "relabel_batch");

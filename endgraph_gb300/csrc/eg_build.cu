@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <thread>
 
 #include "eg_common.cuh"
@@ -261,8 +262,8 @@ __global__ void __launch_bounds__(256) k_scatter(const uint8_t* __restrict__ edg
 }
 
 // ---- outgoing_adj_bitmap (core/graph.hpp:1304-1352): one warp per 64-bit word ---------------
-__global__ void __launch_bounds__(256) k_bitmap(const uint32_t* __restrict__ cnt, uint32_t V, int P,
-                                                 uint64_t* __restrict__ bitmap, uint64_t nwords) {
+__device__ __forceinline__ void bitmap_words(const uint32_t* __restrict__ cnt, uint32_t V, int P,
+                                             uint64_t* __restrict__ bitmap, uint64_t nwords) {
     const int lane = threadIdx.x & 31;
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
     const uint64_t stride = P == 1 ? 0 : (uint64_t)V + 1;
@@ -275,6 +276,10 @@ __global__ void __launch_bounds__(256) k_bitmap(const uint32_t* __restrict__ cnt
         uint32_t b1 = __ballot_sync(0xffffffffu, c1 > 0);
         if (lane == 0) bitmap[wi] = ((uint64_t)b1 << 32) | b0;
     }
+}
+__global__ void __launch_bounds__(256) k_bitmap(const uint32_t* __restrict__ cnt, uint32_t V, int P,
+                                                 uint64_t* __restrict__ bitmap, uint64_t nwords) {
+    bitmap_words(cnt, V, P, bitmap, nwords);
 }
 
 // part_edges[p] = off[p*(V+1)] (after the scatter: start of partition p), part_edges[P] = E
@@ -301,14 +306,14 @@ constexpr int kBuildUnroll = 4;
 
 // Records holding an id >= V are counted nowhere (pass B skips the same records) and raise *bad:
 // a load that uploads and builds in one pipeline validates here instead of in a separate pass.
+// One block `blk` of pass A (s_h: 2 nb shared counters)
 template <int REC>
-__global__ void __launch_bounds__(kBucketThreads) k_bucket_hist(const uint8_t* __restrict__ edges, uint64_t E,
-                                                                 uint64_t chunk, int shift, uint32_t nb, uint32_t nblk,
-                                                                 uint32_t* __restrict__ cnt, uint32_t V, int* bad) {
-    extern __shared__ uint32_t s_h[];  // [2][nb]
+__device__ __forceinline__ void bucket_hist_block(const uint8_t* __restrict__ edges, uint64_t E, uint64_t chunk,
+                                                  int shift, uint32_t nb, uint32_t nblk, uint32_t* __restrict__ cnt,
+                                                  uint32_t V, int* bad, uint32_t blk, uint32_t* s_h) {
     for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_h[i] = 0;
     __syncthreads();
-    const uint64_t e0 = blockIdx.x * chunk;
+    const uint64_t e0 = blk * chunk;
     const uint64_t e1 = e0 + chunk < E ? e0 + chunk : E;
     bool out_of_range = false;
     auto count = [&](uint32_t s, uint32_t d) {
@@ -343,7 +348,15 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_hist(const uint8_t* _
     if (out_of_range) atomicExch(bad, 1);
     __syncthreads();
     // bucket-major layout: [half][bucket][block]
-    for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) cnt[(uint64_t)i * nblk + blockIdx.x] = s_h[i];
+    for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) cnt[(uint64_t)i * nblk + blk] = s_h[i];
+}
+
+template <int REC>
+__global__ void __launch_bounds__(kBucketThreads) k_bucket_hist(const uint8_t* __restrict__ edges, uint64_t E,
+                                                                 uint64_t chunk, int shift, uint32_t nb, uint32_t nblk,
+                                                                 uint32_t* __restrict__ cnt, uint32_t V, int* bad) {
+    extern __shared__ uint32_t s_h[];  // [2][nb]
+    bucket_hist_block<REC>(edges, E, chunk, shift, nb, nblk, cnt, V, bad, blockIdx.x, s_h);
 }
 
 // in-place exclusive scan of s[0..n) by the whole block; returns the total.  s_warp: 33 words
@@ -399,19 +412,19 @@ __host__ __device__ constexpr int scatter_tile(int rec) { return kScatterThreads
 
 // kCheck: skip records with an id >= V as pass A did (an upload validated in pass A); edge lists
 // validated at load leave it off
+// One block `blk` of pass B (s_raw: the bucket tables and the staging tile)
 template <int REC, bool kCheck>
-__global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_t* __restrict__ edges, uint64_t E,
-                                                                    uint64_t chunk, int shift, uint32_t nb, uint32_t nblk,
-                                                                    const uint64_t* __restrict__ excl,
-                                                                    uint8_t* __restrict__ out, uint32_t V) {
+__device__ __forceinline__ void bucket_scatter_block(const uint8_t* __restrict__ edges, uint64_t E, uint64_t chunk,
+                                                     int shift, uint32_t nb, uint32_t nblk,
+                                                     const uint64_t* __restrict__ excl, uint8_t* __restrict__ out,
+                                                     uint32_t V, uint32_t blk, unsigned char* s_raw) {
     constexpr int W = REC / 4;  // words per record
-    extern __shared__ __align__(16) unsigned char s_raw[];
     unsigned long long* s_base = reinterpret_cast<unsigned long long*>(s_raw);  // [2][nb]
     uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_base + 2 * nb);            // [nb]
     uint32_t* s_stage = reinterpret_cast<uint32_t*>(s_raw + align16(20ull * nb));  // [tile][W]
     __shared__ uint32_t s_warp[33];
-    for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_base[i] = excl[(uint64_t)i * nblk + blockIdx.x];
-    const uint64_t e0 = blockIdx.x * chunk;
+    for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_base[i] = excl[(uint64_t)i * nblk + blk];
+    const uint64_t e0 = blk * chunk;
     const uint64_t e1 = e0 + chunk < E ? e0 + chunk : E;
     constexpr int kPer = scatter_per(REC);
     unsigned long long keep;
@@ -488,6 +501,15 @@ __global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_
     }
 }
 
+template <int REC, bool kCheck>
+__global__ void __launch_bounds__(kScatterThreads) k_bucket_scatter(const uint8_t* __restrict__ edges, uint64_t E,
+                                                                    uint64_t chunk, int shift, uint32_t nb, uint32_t nblk,
+                                                                    const uint64_t* __restrict__ excl,
+                                                                    uint8_t* __restrict__ out, uint32_t V) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    bucket_scatter_block<REC, kCheck>(edges, E, chunk, shift, nb, nblk, excl, out, V, blockIdx.x, s_raw);
+}
+
 // Visit records [r0, r1) of a bucket with several loads in flight per thread.  8-byte records go
 // as 16-byte pairs when the buffer is 16-byte aligned (vec); a pair straddling r0 or r1 visits
 // only its in-range half.
@@ -549,20 +571,18 @@ struct BuildParts {
     uint32_t nblk[kMaxParts];
 };
 
-// C: one bucket per CTA iteration (persistent CTAs take buckets from a ticket)
+// C: one bucket per CTA iteration (persistent CTAs take buckets from a ticket); s_cnt: LB counters
 template <int REC>
-__global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* __restrict__ rec, BuildParts parts,
-                                                                 int half, uint32_t nb, uint32_t LB, uint32_t V,
-                                                                 uint32_t* __restrict__ deg, uint64_t* __restrict__ off,
-                                                                 uint32_t* __restrict__ adj, float* __restrict__ wout,
-                                                                 uint32_t* ticket) {
+__device__ __forceinline__ void bucket_build_loop(const uint8_t* __restrict__ rec, const BuildParts& parts, int half,
+                                                  uint32_t nb, uint32_t LB, uint32_t V, uint32_t* __restrict__ deg,
+                                                  uint64_t* __restrict__ off, uint32_t* __restrict__ adj,
+                                                  float* __restrict__ wout, uint32_t* ticket, uint32_t* s_cnt) {
     const bool vec = REC == 8;  // the bucketed buffer is 16-byte aligned
     const bool key_is_src = half == 0;
     // the 4-byte placement stores land at random positions of the bucket's window: ask L2 to keep
     // those lines so that a partly written sector is usually completed before it is evicted
     unsigned long long keep;
     asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(keep));
-    extern __shared__ uint32_t s_cnt[];  // LB counters
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_b;
     __shared__ uint64_t s_lo[kMaxParts], s_hi[kMaxParts];
@@ -611,6 +631,16 @@ __global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* _
             });
         __syncthreads();
     }
+}
+
+template <int REC>
+__global__ void __launch_bounds__(kBuildThreads) k_bucket_build(const uint8_t* __restrict__ rec, BuildParts parts,
+                                                                 int half, uint32_t nb, uint32_t LB, uint32_t V,
+                                                                 uint32_t* __restrict__ deg, uint64_t* __restrict__ off,
+                                                                 uint32_t* __restrict__ adj, float* __restrict__ wout,
+                                                                 uint32_t* ticket) {
+    extern __shared__ uint32_t s_cnt[];  // LB counters
+    bucket_build_loop<REC>(rec, parts, half, nb, LB, V, deg, off, adj, wout, ticket, s_cnt);
 }
 
 struct BucketPlan {
@@ -785,6 +815,322 @@ static int build_single(eg_graph* g, const UploadParts* up) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// The one-partition bucketed build in one cooperative launch: every phase of build_single and of
+// the index kernels of build_structures, separated by bounded grid barriers (grid_sync_bounded),
+// with one 1,024-thread CTA per SM taking pass-A and pass-B blocks by stride, pass-C buckets by
+// ticket and the scans as contiguous ranges.  A graph batch's ids are moved to the union first.
+constexpr int kPersistBuildMaxCtas = 1024;
+
+struct BuildWords {
+    unsigned bar_count, bar_gen;
+    int err;              // a bounded barrier wait gave up
+    int bad;              // a record holds an id out of range
+    uint32_t ticket[2];   // pass-C bucket tickets, per half
+    uint64_t cstart[2];   // entry ranges of the compressed index (cstart[1]: entries + sentinel)
+    uint64_t tot[kPersistBuildMaxCtas];  // per-CTA sums of a grid scan
+};
+
+struct PersistBuildArgs {
+    uint8_t* edges;
+    uint64_t E;
+    uint32_t V;
+    const uint64_t* eoff;  // graph batch: record offsets (G + 1), null for one graph
+    const uint64_t* voff;  // graph batch: vertex offsets (G + 1)
+    uint32_t G;
+    uint64_t chunk;
+    int shift;
+    uint32_t nb, nblk, LB;
+    uint32_t* cnt;
+    uint64_t* ex;
+    uint8_t* bucketed;
+    BuildParts parts;
+    uint32_t *outdeg, *indeg;
+    uint64_t *csr_off, *csc_off;
+    uint32_t *csr_adj, *csc_adj;
+    float *csr_w, *csc_w;
+    uint64_t* bitmap;
+    uint64_t nwords;
+    uint32_t* cvert;
+    uint64_t* cidx;
+    BuildWords* w;
+};
+
+__device__ __forceinline__ bool build_barrier(BuildWords* w) { return grid_sync_bounded(&w->bar_count, &w->bar_gen, &w->err); }
+
+__device__ __forceinline__ uint64_t block_sum_u64(uint64_t v, uint64_t* s_red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = warp_sum_u64(v);
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        uint64_t x = lane < (int)(blockDim.x >> 5) ? s_red[lane] : 0ull;
+        x = warp_sum_u64(x);
+        if (lane == 0) s_red[32] = x;
+    }
+    __syncthreads();
+    const uint64_t r = s_red[32];
+    __syncthreads();
+    return r;
+}
+
+// exclusive prefix of one value per thread over the block; *total: the block's sum
+__device__ __forceinline__ uint64_t block_excl_u64(uint64_t v, uint64_t* s_red, uint64_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint64_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) s_red[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint64_t x = lane < nw ? s_red[lane] : 0ull;
+        uint64_t y = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t z = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= o) y += z;
+        }
+        if (lane < nw) s_red[lane] = y - x;
+        if (lane == 31) s_red[32] = y;
+    }
+    __syncthreads();
+    const uint64_t r = s_red[warp] + inc - v;
+    *total = s_red[32];
+    __syncthreads();
+    return r;
+}
+
+// Exclusive scan of n u32 values over the whole grid without look-back: each CTA sums its own
+// contiguous range, a grid barrier, then each CTA rescans its range from the sum of the earlier
+// ranges and hands every item its exclusive prefix (epi(i, excl, value)).  *total_out (optional)
+// gets the sum of all.  False when the barrier gave up.
+template <class Load, class Epi>
+__device__ bool grid_scan(Load load, Epi epi, uint64_t n, BuildWords* w, uint64_t* total_out) {
+    __shared__ uint64_t s_red[33];
+    const uint64_t L = (n + gridDim.x - 1) / gridDim.x;
+    const uint64_t lo = min(n, (uint64_t)blockIdx.x * L), hi = min(n, lo + L);
+    uint64_t sum = 0;
+    for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) sum += load(i);
+    sum = block_sum_u64(sum, s_red);
+    if (threadIdx.x == 0) w->tot[blockIdx.x] = sum;
+    if (!build_barrier(w)) return false;
+    uint64_t p = 0;
+    for (uint32_t c = threadIdx.x; c < blockIdx.x; c += blockDim.x) p += __ldcg(&w->tot[c]);
+    p = block_sum_u64(p, s_red);
+    if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total_out = p + __ldcg(&w->tot[blockIdx.x]);
+    constexpr int kPer = 4;
+    for (uint64_t t0 = lo; t0 < hi; t0 += (uint64_t)blockDim.x * kPer) {
+        const uint64_t b = t0 + (uint64_t)threadIdx.x * kPer;
+        uint32_t v[kPer];
+        uint64_t ts = 0;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            v[j] = b + j < hi ? load(b + j) : 0u;
+            ts += v[j];
+        }
+        uint64_t tile_total;
+        uint64_t run = p + block_excl_u64(ts, s_red, &tile_total);
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            if (b + j < hi) epi(b + j, run, v[j]);
+            run += v[j];
+        }
+        p += tile_total;
+    }
+    return true;
+}
+
+// Union ids of a graph batch: record i of graph k (eoff[k] <= i < eoff[k+1]) gets voff[k] added to
+// both ids, once they are checked against the graph's vertex count (*bad otherwise).  Loads and
+// stores go to L2 only, so that no SM holds a stale L1 line of the records for the passes that
+// read them later in the same launch.
+template <int REC>
+__device__ void relabel_union(uint8_t* edges, uint64_t E, const uint64_t* __restrict__ eoff,
+                              const uint64_t* __restrict__ voff, uint32_t G, int* bad) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    bool out_of_range = false;
+    uint32_t lo = 0;  // graph of the previous record of this thread (records only move forward)
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < E; i += stride) {
+        if (lo + 1 < G && __ldg(eoff + lo + 1) <= i) {
+            uint32_t hi = G;  // last graph with eoff <= i, searched in (lo, G)
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (__ldg(eoff + mid) <= i) lo = mid; else hi = mid;
+            }
+        }
+        uint32_t* r = reinterpret_cast<uint32_t*>(edges + i * (uint64_t)REC);
+        const uint32_t s = __ldcg(r), d = __ldcg(r + 1);
+        const uint64_t base = __ldg(voff + lo), nv = __ldg(voff + lo + 1) - base;
+        if (s >= nv || d >= nv) {
+            out_of_range = true;
+            continue;
+        }
+        __stcg(r, (uint32_t)(base + s));
+        __stcg(r + 1, (uint32_t)(base + d));
+    }
+    if (out_of_range) atomicExch(bad, 1);
+}
+
+template <int REC>
+__global__ void __launch_bounds__(kBuildThreads, 1) k_build_persistent(PersistBuildArgs a) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    BuildWords* w = a.w;
+    if (a.eoff) {
+        relabel_union<REC>(a.edges, a.E, a.eoff, a.voff, a.G, &w->bad);
+        if (!build_barrier(w)) return;
+    }
+    // A: bucket counts per (half, bucket, block)
+    for (uint32_t blk = blockIdx.x; blk < a.nblk; blk += gridDim.x) {
+        bucket_hist_block<REC>(a.edges, a.E, a.chunk, a.shift, a.nb, a.nblk, a.cnt, a.V, &w->bad, blk,
+                               reinterpret_cast<uint32_t*>(s_raw));
+        __syncthreads();
+    }
+    if (!build_barrier(w)) return;
+    if (*(volatile int*)&w->bad) return;  // every CTA reads the same flag after the barrier
+    const uint64_t ncnt = 2ull * a.nb * a.nblk;
+    if (!grid_scan(LoadU32{a.cnt}, EpiExclusive{a.ex}, ncnt, w, a.ex + ncnt)) return;
+    if (!build_barrier(w)) return;
+    // B: records bucket-sorted per half
+    for (uint32_t blk = blockIdx.x; blk < a.nblk; blk += gridDim.x) {
+        bucket_scatter_block<REC, false>(a.edges, a.E, a.chunk, a.shift, a.nb, a.nblk, a.ex, a.bucketed, a.V, blk,
+                                         s_raw);
+        __syncthreads();
+    }
+    if (!build_barrier(w)) return;
+    // C: both halves (independent outputs, no barrier between them)
+    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_raw);
+    bucket_build_loop<REC>(a.bucketed, a.parts, 0, a.nb, a.LB, a.V, a.outdeg, a.csr_off, a.csr_adj, a.csr_w,
+                           &w->ticket[0], s_cnt);
+    __syncthreads();  // every thread has read the last ticket of half 0 before thread 0 takes one of half 1
+    bucket_build_loop<REC>(a.bucketed, a.parts, 1, a.nb, a.LB, a.V, a.indeg, a.csc_off, a.csc_adj, a.csc_w,
+                           &w->ticket[1], s_cnt);
+    if (!build_barrier(w)) return;
+    // outgoing_adj_bitmap and the compressed incoming index
+    bitmap_words(a.outdeg, a.V, 1, a.bitmap, a.nwords);
+    grid_scan(LoadFlag{a.indeg, a.V, 1}, EpiCompress{a.csc_off, a.cvert, a.cidx, w->cstart, a.V, 1, a.indeg},
+              (uint64_t)a.V + 1, w, nullptr);
+}
+
+bool persistent_build_fits(const eg_graph* g) {
+    return g->partitions == 1 && g->sub_partitions == 1 && g->E > 0 &&
+           align16(20ull * plan_buckets(g->V, g->E).nb) + (uint64_t)scatter_tile(g->edge_bytes) * g->edge_bytes <=
+               200ull * 1024;
+}
+
+int build_persistent(eg_graph* g, const uint64_t* eoff, const uint64_t* voff, uint32_t G) {
+    const uint32_t V = g->V;
+    const uint64_t E = g->E;
+    const int rec = g->edge_bytes;
+    if (!persistent_build_fits(g)) {
+        set_error("eg_build: the one-launch build needs one partition, one sub-partition and edges");
+        return EG_ERR_UNSUPPORTED;
+    }
+    g->built_csr = g->built_csc = false;
+    g->eng.pull_ready = false;
+    g->eng.pr_ready = false;
+    const BucketPlan q = plan_buckets(V, E);
+    const uint64_t ncnt = 2ull * q.nb * q.nblk;
+    const uint64_t nwords = (uint64_t)V / 64 + 1;
+    EG_TRY(g->outdeg.reserve(sizeof(uint32_t) * (size_t)V));
+    EG_TRY(g->indeg.reserve(sizeof(uint32_t) * (size_t)V));
+    EG_TRY(g->csr_off.reserve(sizeof(uint64_t) * ((size_t)V + 1)));
+    EG_TRY(g->csc_off.reserve(sizeof(uint64_t) * ((size_t)V + 1)));
+    EG_TRY(g->csr_adj.reserve(sizeof(uint32_t) * (E + 32)));
+    EG_TRY(g->csc_adj.reserve(sizeof(uint32_t) * (E + 32)));
+    if (g->weighted) {
+        EG_TRY(g->csr_w.reserve(sizeof(float) * (E + 32)));
+        EG_TRY(g->csc_w.reserve(sizeof(float) * (E + 32)));
+    }
+    EG_TRY(g->bucket_cnt.reserve(sizeof(uint32_t) * ncnt));
+    EG_TRY(g->bucket_off.reserve(sizeof(uint64_t) * (ncnt + 1)));
+    EG_TRY(g->bucketed.reserve((size_t)2 * E * rec + 64));
+    EG_TRY(g->csr_bitmap.reserve(sizeof(uint64_t) * nwords));
+    const uint64_t cap = std::min<uint64_t>(E, V) + 1;
+    EG_TRY(g->cvert.reserve(sizeof(uint32_t) * cap));
+    EG_TRY(g->cidx.reserve(sizeof(uint64_t) * cap));
+    EG_TRY(g->build_words.reserve(sizeof(BuildWords)));
+    BuildWords* w = g->build_words.as<BuildWords>();
+    EG_CUDA(cudaMemsetAsync(w, 0, sizeof(BuildWords), g->stream));
+
+    const size_t smem = std::max({sizeof(uint32_t) * 2 * q.nb, align16(20ull * q.nb) + (size_t)scatter_tile(rec) * rec,
+                                  sizeof(uint32_t) * (size_t)q.LB});
+    const void* fn = rec == 8 ? (const void*)k_build_persistent<8> : (const void*)k_build_persistent<12>;
+    EG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBuildThreads, smem));
+    const int grid = std::min(g->num_sms * per_sm, kPersistBuildMaxCtas);
+    if (grid < 1) {
+        set_error("eg_build: the one-launch build does not fit an SM");
+        return EG_ERR_UNSUPPORTED;
+    }
+    PersistBuildArgs a;
+    a.edges = g->edges.as<uint8_t>();
+    a.E = E;
+    a.V = V;
+    a.eoff = eoff;
+    a.voff = voff;
+    a.G = G;
+    a.chunk = q.chunk;
+    a.shift = q.shift;
+    a.nb = q.nb;
+    a.nblk = q.nblk;
+    a.LB = q.LB;
+    a.cnt = g->bucket_cnt.as<uint32_t>();
+    a.ex = g->bucket_off.as<uint64_t>();
+    a.bucketed = g->bucketed.as<uint8_t>();
+    a.parts = BuildParts{};
+    a.parts.K = 1;
+    a.parts.base2[0] = 0;
+    a.parts.excl[0] = a.ex;
+    a.parts.nblk[0] = q.nblk;
+    a.outdeg = g->outdeg.as<uint32_t>();
+    a.indeg = g->indeg.as<uint32_t>();
+    a.csr_off = g->csr_off.as<uint64_t>();
+    a.csc_off = g->csc_off.as<uint64_t>();
+    a.csr_adj = g->csr_adj.as<uint32_t>();
+    a.csc_adj = g->csc_adj.as<uint32_t>();
+    a.csr_w = g->csr_w.as<float>();
+    a.csc_w = g->csc_w.as<float>();
+    a.bitmap = g->csr_bitmap.as<uint64_t>();
+    a.nwords = nwords;
+    a.cvert = g->cvert.as<uint32_t>();
+    a.cidx = g->cidx.as<uint64_t>();
+    a.w = w;
+    void* kargs[] = {&a};
+    {
+        Timed t(&g->prof, g->stream, "build_persistent");
+        EG_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3(kBuildThreads), kargs, smem, g->stream));
+        EG_CHECK_LAUNCH("k_build_persistent");
+    }
+    BuildWords hw;  // the flags and the index range (the per-CTA sums are not needed)
+    EG_CUDA(cudaMemcpyAsync(&hw, w, offsetof(BuildWords, tot), cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    if (hw.err) {
+        set_error("eg_build: a bounded grid barrier of the one-launch build gave up");
+        return EG_ERR_TIMEOUT;
+    }
+    if (hw.bad) {
+        set_error(eoff ? "eg_load_graph_batch: a record holds a vertex id >= its graph's vertex count"
+                       : "edge list holds a vertex id >= V (%u)", V);
+        return EG_ERR_INVALID;
+    }
+    // one partition, one sub-partition: the CPBT boundaries are [0, V]
+    g->part_off.assign({0u, V});
+    g->local_off.assign({0u, V});
+    EG_TRY(g->d_part_off.reserve(sizeof(uint32_t) * 2));
+    EG_CUDA(cudaMemcpyAsync(g->d_part_off.ptr, g->part_off.data(), sizeof(uint32_t) * 2, cudaMemcpyHostToDevice, g->stream));
+    g->part_edges_csr.assign({0ull, E});
+    g->part_edges_csc.assign({0ull, E});
+    g->cstart.assign({0ull, hw.cstart[1]});
+    g->ncompressed = hw.cstart[1];
+    EG_CUDA(cudaStreamSynchronize(g->stream));
+    g->built_csr = g->built_csc = true;
+    return EG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
 int compute_degrees(eg_graph* g) {
     const uint64_t E = g->E;
     const uint32_t V = g->V;
@@ -906,6 +1252,7 @@ int build_structures(eg_graph* g, int want_csr, int want_csc, const UploadParts*
     g->eng.pull_ready = false;
     g->eng.pr_ready = false;
 
+    if (g->build_launch && !up && persistent_build_fits(g)) return build_persistent(g, nullptr, nullptr, 0);
     // the bucket tables and a staging tile must fit one CTA's shared memory
     const bool bucketed =
         P == 1 && align16(20ull * plan_buckets(V, E).nb) + (uint64_t)scatter_tile(g->edge_bytes) * g->edge_bytes <=

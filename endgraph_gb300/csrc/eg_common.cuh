@@ -165,6 +165,7 @@ struct eg_graph {
     eg::DevBuf tmp64;  // generic u64 scratch
     eg::DevBuf cpbt_scratch;
     eg::DevBuf bucket_cnt, bucket_off, bucketed;  // one-partition bucketed build
+    eg::DevBuf build_words;  // barrier, tickets and flags of the one-launch build
     eg::DevBuf err;    // device error flags (int)
     eg::EngineState eng;
     eg::Profiler prof;
@@ -185,6 +186,7 @@ struct eg_graph {
     int use_cuda_graph = 0; // batched BFS: replay the level loop as one captured CUDA graph
     int batch_launch = 0;   // batched BFS: 1 runs every level inside one persistent launch
     int batch_div = 0;      // batched BFS switch divisor; 0: the same as dense_div
+    int build_launch = 0;   // 1: a one-partition build runs as one persistent cooperative launch
     int pull_blocks_per_sm = 0;  // pull-sweep grid; 0 = occupancy limit
     int batch_width = 64;        // roots per bit-parallel pass (eg_bfs_many)
     int pr_relabel = -1;         // PageRank gathers through renumbered sources: 1 on, 0 off, -1 automatic
@@ -216,6 +218,10 @@ struct UploadParts {
     const std::atomic<bool>* failed = nullptr;
 };
 int build_structures(eg_graph* g, int want_csr, int want_csc, const UploadParts* up = nullptr);
+// the one-partition, one-sub-partition build as one cooperative launch; eoff / voff (device, G + 1
+// entries each, optional): a graph batch whose ids are moved to the union inside the launch
+bool persistent_build_fits(const eg_graph* g);
+int build_persistent(eg_graph* g, const uint64_t* eoff, const uint64_t* voff, uint32_t G);
 // eg_load_directed of host records from this many records on: upload and build pipelined
 constexpr uint64_t kPipelinedLoadMin = 1ull << 22;
 int load_build_pipelined(eg_graph* g, const void* edges, uint64_t E, uint32_t V, int edge_bytes);
@@ -250,6 +256,41 @@ int load_graph_batch(eg_graph* g, const void* edges, int rec, const uint64_t* eo
 int run_msbfs_graphs(eg_graph* g, const uint32_t* roots, int nper, uint8_t* levels, int where, uint64_t* edges);
 int run_sssp_graphs(eg_graph* g, const uint32_t* sources, int nper, float* dist, int where);
 int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E);
+
+// Bounded grid barrier of a cooperative launch (every CTA resident).  count and gen start at zero;
+// the last CTA to arrive resets count and advances gen, the others poll gen.  A poll that runs
+// past kBarrierSpinCap, or that sees *err already raised by another CTA, raises *err and returns
+// false: the caller leaves the kernel, so no CTA waits forever on one that left.
+constexpr uint32_t kBarrierSpinCap = 1u << 22;
+__device__ __forceinline__ bool grid_sync_bounded(unsigned* count, unsigned* gen, int* err) {
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        const unsigned nblocks = gridDim.x;
+        const unsigned g0 = *(volatile unsigned*)gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(count, 1u) == nblocks - 1) {
+            atomicExch(count, 0u);
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            uint32_t spins = 0;
+            while (*(volatile unsigned*)gen == g0) {
+                if (++spins > kBarrierSpinCap || *(volatile int*)err) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
 
 // the push/pull switch of the batched traversals: sparse iff the frontier's out-edges < E / this
 inline int batch_divisor(const eg_graph* g) { return g->batch_div > 0 ? g->batch_div : g->dense_div; }

@@ -113,10 +113,6 @@ int check_device_error(eg_graph* g, const char* what) {
 
 // ---------------------------------------------------------------------------------------------
 // scan of u32 counts into inclusive u64 offsets: out[i] = sum(in[0..i]), out[n] = total
-struct LoadU32 {
-    const uint32_t* p;
-    __device__ uint32_t operator()(uint64_t i) const { return p[i]; }
-};
 struct EpiInclusive {
     uint64_t* out;
     __device__ void operator()(uint64_t i, uint64_t excl, uint32_t v) const { out[i] = excl + v; }
@@ -126,10 +122,6 @@ int scan_u32_to_u64(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out_i
     return launch_scan(g, LoadU32{in}, EpiInclusive{out_incl}, n, total_dev, "scan_offsets");
 }
 
-struct EpiExclusive {
-    uint64_t* out;
-    __device__ void operator()(uint64_t i, uint64_t excl, uint32_t) const { out[i] = excl; }
-};
 
 // out[i] = sum(in[0..i)), out[n] = total
 int scan_exclusive_u32(eg_graph* g, const uint32_t* in, uint64_t n, uint64_t* out) {
@@ -161,33 +153,6 @@ int selftest_bounded_wait(eg_graph* g, uint32_t spin_cap) {
 // compressed incoming index (core/graph.hpp:1144-1188): one (vertex, start) per non-empty list
 // (p, v) plus a sentinel (V, partition end) per partition; cnt holds P*(V+1) counts with the
 // (V+1)-th slot of each partition as the sentinel slot.
-struct LoadFlag {
-    const uint32_t* cnt;
-    uint32_t V;
-    int single;  // P == 1: cnt has V entries, slot V is the sentinel
-    __device__ uint32_t operator()(uint64_t i) const {
-        uint64_t r = single ? i : i % ((uint64_t)V + 1);
-        if (r == V) return 1u;
-        return cnt[i] > 0 ? 1u : 0u;
-    }
-};
-struct EpiCompress {
-    const uint64_t* off;
-    uint32_t* cvert;
-    uint64_t* cidx;
-    uint64_t* cstart;
-    uint32_t V;
-    int single;
-    const uint32_t* cnt;
-    __device__ void operator()(uint64_t i, uint64_t excl, uint32_t flag) const {
-        if (!flag) return;
-        uint64_t r = single ? i : i % ((uint64_t)V + 1);
-        cvert[excl] = r == V ? V : (uint32_t)r;
-        cidx[excl] = off[i];
-        if (r == V) cstart[single ? 1 : i / ((uint64_t)V + 1) + 1] = excl + 1;
-    }
-};
-
 int compress_index(eg_graph* g, const uint32_t* cnt, uint64_t n, uint32_t V, const uint64_t* off, uint32_t* cvert,
                    uint64_t* cidx, uint64_t* cstart_dev) {
     int single = n == (uint64_t)V + 1;

@@ -205,8 +205,13 @@ enum {
                                       with the push/pull switch and the queue lengths on the
                                       device; bounded grid barriers); 0 the host-driven loop or,
                                       with EG_OPT_CUDA_GRAPH, the captured one */
-    EG_OPT_BATCH_DIVISOR = 10      /* the switch of the batched BFS (push iff the union frontier's
+    EG_OPT_BATCH_DIVISOR = 10,     /* the switch of the batched BFS (push iff the union frontier's
                                       out-edges < E / divisor); 0 (the default): EG_OPT_DENSE_DIVISOR */
+    EG_OPT_BUILD_LAUNCH = 11       /* the next one-partition, one-sub-partition build from device
+                                      records (eg_build, eg_load_graph_batch): 1 runs it as one
+                                      persistent cooperative launch (batch id relabel, the three
+                                      bucket passes, bitmap and compressed index between bounded grid
+                                      barriers); 0 (the default): one launch per pass */
 };
 int eg_set_option(eg_graph* g, int option, int64_t value);
 

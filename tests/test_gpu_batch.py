@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import rel_l1, rmat_graph
+from helpers import graph_batch, rel_l1, rmat_graph
 
 pytestmark = pytest.mark.gpu
 
@@ -103,28 +103,12 @@ def test_autotune_keeps_results(eg_lib):
             assert np.array_equal(levels[s], np.where(ref == oracle.UNREACHED, 255, ref).astype(np.uint8))
 
 
-def _graph_batch(G, seed, weighted=False):
-    rng = np.random.default_rng(seed)
-    Vs = np.exp(rng.uniform(np.log(100), np.log(5000), G)).astype(np.uint32)
-    efs = rng.integers(4, 33, G)
-    parts = []
-    for i in range(G):
-        s, d, w = rmat_graph(int(Vs[i]), int(Vs[i] * efs[i]), seed * 1000 + i, weights=(0.0, 1.0) if weighted else None)
-        parts.append((s, d, w))
-    eoff = np.zeros(G + 1, np.uint64)
-    eoff[1:] = np.cumsum([len(p[0]) for p in parts])
-    src = np.concatenate([p[0] for p in parts])
-    dst = np.concatenate([p[1] for p in parts])
-    w = np.concatenate([p[2] for p in parts]) if weighted else None
-    return Vs, eoff, parts, src, dst, w
-
-
 @pytest.mark.parametrize("cuda_graph,persistent", [(0, 0), (1, 0), (0, 1)])
 def test_graph_batch_msbfs(eg_lib, cuda_graph, persistent):
     """Many small graphs preprocessed together; 64 roots per graph; every graph matches the oracle."""
     import endgraph_gb300 as eg
     G = 40
-    Vs, eoff, parts, src, dst, _ = _graph_batch(G, 7)
+    Vs, eoff, parts, src, dst, _ = graph_batch(G, 7)
     rng = np.random.default_rng(1)
     roots = np.concatenate([rng.integers(0, Vs[i], 64) for i in range(G)]).astype(np.uint32)
     with eg.Graph() as g:
@@ -147,7 +131,7 @@ def test_graph_batch_msbfs(eg_lib, cuda_graph, persistent):
 def test_graph_batch_sssp(eg_lib):
     import endgraph_gb300 as eg
     G = 24
-    Vs, eoff, parts, src, dst, w = _graph_batch(G, 8, weighted=True)
+    Vs, eoff, parts, src, dst, w = graph_batch(G, 8, weighted=True)
     rng = np.random.default_rng(2)
     sources = np.concatenate([rng.integers(0, Vs[i], 64) for i in range(G)]).astype(np.uint32)
     with eg.Graph() as g:
