@@ -186,7 +186,7 @@ struct eg_graph {
     int use_cuda_graph = 0; // batched BFS: replay the level loop as one captured CUDA graph
     int batch_launch = 0;   // batched BFS: 1 runs every level inside one persistent launch
     int batch_div = 0;      // batched BFS switch divisor; 0: the same as dense_div
-    int build_launch = 0;   // 1: a one-partition build runs as one persistent cooperative launch
+    int build_launch = 1;   // 1: a one-partition build runs as one persistent cooperative launch
     int pull_blocks_per_sm = 0;  // pull-sweep grid; 0 = occupancy limit
     int batch_width = 64;        // roots per bit-parallel pass (eg_bfs_many)
     int pr_relabel = -1;         // PageRank gathers through renumbered sources: 1 on, 0 off, -1 automatic

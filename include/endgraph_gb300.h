@@ -209,9 +209,9 @@ enum {
                                       out-edges < E / divisor); 0 (the default): EG_OPT_DENSE_DIVISOR */
     EG_OPT_BUILD_LAUNCH = 11       /* the next one-partition, one-sub-partition build from device
                                       records (eg_build, eg_load_graph_batch): 1 runs it as one
-                                      persistent cooperative launch (batch id relabel, the three
-                                      bucket passes, bitmap and compressed index between bounded grid
-                                      barriers); 0 (the default): one launch per pass */
+                                      persistent cooperative launch (the default: batch id relabel,
+                                      the three bucket passes, bitmap and compressed index between
+                                      bounded grid barriers); 0: one launch per pass */
 };
 int eg_set_option(eg_graph* g, int option, int64_t value);
 

@@ -1,8 +1,8 @@
-"""The one-partition build as one persistent cooperative launch (EG_OPT_BUILD_LAUNCH = 1): the same
-degrees, CPBT boundaries, CSR, CSC, outgoing bitmap and compressed incoming index as the build with
-one launch per pass, and as the oracle, for one graph and for a batch of graphs (whose ids move to
-the union inside the launch); the traversals that follow see a complete graph; ids out of range
-are refused and leave the handle usable."""
+"""The one-partition build as one persistent cooperative launch (EG_OPT_BUILD_LAUNCH = 1, the
+default) gives the same degrees, CPBT boundaries, CSR, CSC, outgoing bitmap and compressed incoming
+index as the build with one launch per pass (EG_OPT_BUILD_LAUNCH = 0) and as the oracle, for one
+graph and for a batch of graphs (whose ids move to the union inside the launch); the traversals
+that follow see a complete graph; ids out of range are refused and leave the handle usable."""
 import numpy as np
 import pytest
 
@@ -51,6 +51,7 @@ def test_one_launch_build_single_graph(eg_lib, weighted):
     src, dst, w = rmat_graph(V, E, 31, weights=(0.0, 1.0) if weighted else None)
     recs = eg.pack_edges(src, dst, w)
     with eg.Graph() as g:
+        g.set_option(eg.EG_OPT_BUILD_LAUNCH, 0)
         g.load_directed(recs, V)
         per_pass = _structure(g)
         g.set_option(eg.EG_OPT_BUILD_LAUNCH, 1)
@@ -79,6 +80,7 @@ def test_one_launch_build_graph_batch(eg_lib, weighted):
     rng = np.random.default_rng(4)
     roots = np.concatenate([rng.integers(0, Vs[i], 64) for i in range(G)]).astype(np.uint32)
     with eg.Graph() as g:
+        g.set_option(eg.EG_OPT_BUILD_LAUNCH, 0)
         g.load_graph_batch(recs, eoff, Vs)
         per_pass = _structure(g)
         g.set_option(eg.EG_OPT_BUILD_LAUNCH, 1)
