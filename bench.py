@@ -255,6 +255,8 @@ ALG_BYTES = {  # algorithmic bytes per launch (E edges, V vertices, nc compresse
     "bucket_hist": lambda E, V, nc: 8 * E,
     "bucket_scatter": lambda E, V, nc: 24 * E,
     "bucket_build": lambda E, V, nc: 12 * E + 12 * V,
+    # the whole one-partition preprocessing in one launch: the 24E + 32V of prep_alg_GBps
+    "build_persistent": lambda E, V, nc: 24 * E + 32 * V,
 }
 
 
