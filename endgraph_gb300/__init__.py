@@ -108,6 +108,7 @@ SIGNATURES = {
     "eg_profile_reset": ([_vp], _i32),
     "eg_profile_read": ([_vp, _vp, _i32, _vp], _i32),
     "eg_selftest_bounded_wait": ([_vp, _u32], _i32),
+    "eg_selftest_grid_barrier": ([_vp, _u32], _i32),
     "eg_load_file": ([_vp, ctypes.c_char_p, _u32, _i32, _i32], _i32),
     "eg_load_directed_file": ([_vp, ctypes.c_char_p, _u32, _i32], _i32),
 }
@@ -493,6 +494,11 @@ class Graph:
     def selftest_bounded_wait(self, spin_cap=1000):
         """Status of a look-back scan whose wait is made to run out (EG_ERR_TIMEOUT expected)."""
         return self._L.eg_selftest_bounded_wait(self.h, spin_cap)
+
+    def selftest_grid_barrier(self, spin_cap=1000):
+        """Status of a cooperative launch whose grid barrier is made to run out (EG_ERR_TIMEOUT
+        expected)."""
+        return self._L.eg_selftest_grid_barrier(self.h, spin_cap)
 
     def profile_read(self):
         n = ctypes.c_int()

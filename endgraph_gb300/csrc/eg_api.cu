@@ -920,4 +920,14 @@ int eg_selftest_bounded_wait(eg_graph* g, uint32_t spin_cap) {
     return selftest_bounded_wait(g, spin_cap);
 }
 
+int eg_selftest_grid_barrier(eg_graph* g, uint32_t spin_cap) {
+    EG_TRY(check_graph(g, "eg_selftest_grid_barrier"));
+    if (spin_cap < 1 || spin_cap > (1u << 22)) {
+        set_error("eg_selftest_grid_barrier: spin_cap must be in 1..2^22");
+        return EG_ERR_INVALID;
+    }
+    EG_CUDA(cudaSetDevice(g->device));
+    return selftest_grid_barrier(g, spin_cap);
+}
+
 }  // extern "C"

@@ -232,6 +232,7 @@ int cpbt_device(eg_graph* g, const uint32_t* d_deg, uint32_t V, int P, int S, ui
 int cpbt_search(eg_graph* g, const uint64_t* d_w, uint32_t n, int P, int S, uint32_t* po, uint32_t* lpo);
 int check_device_error(eg_graph* g, const char* what);
 int selftest_bounded_wait(eg_graph* g, uint32_t spin_cap);
+int selftest_grid_barrier(eg_graph* g, uint32_t spin_cap);
 int validate_edges(eg_graph* g, uint64_t E);
 int symmetrize_edges(eg_graph* g, uint64_t E);
 int run_pagerank(eg_graph* g, int iterations, float damping, float* out, int where);
@@ -262,7 +263,8 @@ int expand_with_ids(eg_graph* g, const uint8_t* rec8_dev, uint64_t E);
 // past kBarrierSpinCap, or that sees *err already raised by another CTA, raises *err and returns
 // false: the caller leaves the kernel, so no CTA waits forever on one that left.
 constexpr uint32_t kBarrierSpinCap = 1u << 22;
-__device__ __forceinline__ bool grid_sync_bounded(unsigned* count, unsigned* gen, int* err) {
+__device__ __forceinline__ bool grid_sync_bounded(unsigned* count, unsigned* gen, int* err,
+                                                  uint32_t spin_cap = kBarrierSpinCap) {
     __syncthreads();
     __shared__ int s_ok;
     if (threadIdx.x == 0) {
@@ -277,7 +279,7 @@ __device__ __forceinline__ bool grid_sync_bounded(unsigned* count, unsigned* gen
         } else {
             uint32_t spins = 0;
             while (*(volatile unsigned*)gen == g0) {
-                if (++spins > kBarrierSpinCap || *(volatile int*)err) {
+                if (++spins > spin_cap || *(volatile int*)err) {
                     atomicExch(err, 1);
                     ok = 0;
                     break;

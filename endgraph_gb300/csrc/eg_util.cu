@@ -149,6 +149,26 @@ int selftest_bounded_wait(eg_graph* g, uint32_t spin_cap) {
     return check_device_error(g, "eg_selftest_bounded_wait");
 }
 
+// The bounded grid barrier of the persistent kernels, exercised: a cooperative launch of four CTAs
+// in which CTA 0 never arrives, so the other three poll until spin_cap runs out, raise the error
+// flag and leave; the caller sees EG_ERR_TIMEOUT and the handle stays usable.
+__global__ void k_grid_barrier_selftest(unsigned* words, int* err, uint32_t spin_cap) {
+    if (blockIdx.x == 0) return;
+    grid_sync_bounded(words, words + 1, err, spin_cap);
+}
+
+int selftest_grid_barrier(eg_graph* g, uint32_t spin_cap) {
+    EG_TRY(g->tmp64.reserve(16));
+    unsigned* words = reinterpret_cast<unsigned*>(g->tmp64.ptr);
+    EG_CUDA(cudaMemsetAsync(words, 0, 16, g->stream));
+    EG_CUDA(cudaMemsetAsync(g->err.ptr, 0, sizeof(int), g->stream));
+    int* err = g->err.as<int>();
+    void* kargs[] = {&words, &err, &spin_cap};
+    EG_CUDA(cudaLaunchCooperativeKernel((const void*)k_grid_barrier_selftest, dim3(4), dim3(32), kargs, 0, g->stream));
+    EG_CHECK_LAUNCH("k_grid_barrier_selftest");
+    return check_device_error(g, "eg_selftest_grid_barrier");
+}
+
 // ---------------------------------------------------------------------------------------------
 // compressed incoming index (core/graph.hpp:1144-1188): one (vertex, start) per non-empty list
 // (p, v) plus a sentinel (V, partition end) per partition; cnt holds P*(V+1) counts with the

@@ -293,6 +293,11 @@ int eg_profile_read(eg_graph* g, eg_kernel_stat* out, int cap, int* count);
  * withheld, so the wait of the second tile runs out after spin_cap polls (1 .. 2^22).  Returns
  * EG_ERR_TIMEOUT, as any exhausted wait does, and leaves the handle and its context usable. */
 int eg_selftest_bounded_wait(eg_graph* g, uint32_t spin_cap);
+/* The grid barrier of the persistent launches (the one-launch build, the persistent batched BFS)
+ * is bounded the same way: this call makes a cooperative launch in which one CTA never arrives,
+ * so the others give up after spin_cap polls (1 .. 2^22).  Returns EG_ERR_TIMEOUT and leaves the
+ * handle and its context usable. */
+int eg_selftest_grid_barrier(eg_graph* g, uint32_t spin_cap);
 
 #ifdef __cplusplus
 }

@@ -224,6 +224,23 @@ def test_bounded_wait_runs_out_and_handle_survives(eg_lib):
         assert list(lv) == [0, 1, 2, 3]
 
 
+def test_grid_barrier_runs_out_and_handle_survives(eg_lib):
+    """The bounded grid barrier of the persistent launches: with one CTA that never arrives, the
+    others give up after their poll limit, the call returns EG_ERR_TIMEOUT (no trap, no hang), and
+    the same handle then builds in one persistent launch and traverses."""
+    import endgraph_gb300 as eg
+    src = np.array([0, 1, 2], np.uint32)
+    dst = np.array([1, 2, 3], np.uint32)
+    with eg.Graph() as g:
+        assert g.selftest_grid_barrier(0) == 1  # EG_ERR_INVALID: the poll limit must be >= 1
+        assert g.selftest_grid_barrier(1000) == 5  # EG_ERR_TIMEOUT
+        assert b"bounded device wait" in eg_lib.eg_last_error()
+        g.set_option(eg.EG_OPT_BUILD_LAUNCH, 1)
+        g.load_directed(eg.pack_edges(src, dst), 4)
+        lv, _ = g.bfs(0)
+        assert list(lv) == [0, 1, 2, 3]
+
+
 def test_file_ingest_matches_memory_load(eg_lib, tmp_path):
     """eg_load_file (pieces read into pinned buffers while the previous piece is copied) and
     eg_load_directed_file (read, uploaded and built in parts) load the same graph as the records
