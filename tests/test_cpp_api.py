@@ -128,7 +128,7 @@ def test_host_callbacks_are_refused_loudly(eg_lib, tmp_path):
 PERSIST_PROGRAM = r"""
 #include "core/graph.hpp"
 // Dumps the PageRank result with the header's dump_vertex_array, restores it into a second array
-// and writes both to stdout as a verdict line; checks the reference's file rules on the way.
+// and writes both to stdout as one result line; checks the reference's file rules on the way.
 int main(int argc, char** argv) {
     Graph<Empty> g(1);
     g.load_directed(argv[1], (UINT)atoi(argv[2]));

@@ -21,7 +21,7 @@ def test_optimal_offset_known_answers(oracle_mod):
     a = g["kat_a"]
     for k in (1, 2, 3, 4, 5, 10, 11):
         assert np.array_equal(oracle.optimal_offset(a, k), g[f"kat_a_k{k}"]), k
-    # the survey's hand-checked cases: greedy-furthest hops, zero pages join the left chunk
+    # cases checked by hand: greedy-furthest hops, zero pages join the left chunk
     assert list(g["kat_a_k2"]) == [0, 6, 10]
     assert list(g["kat_a_k4"]) == [0, 3, 6, 7, 10]
     assert list(g["kat_a_k5"]) == [0, 3, 6, 7, 10, 10]
