@@ -124,3 +124,31 @@ def test_one_launch_build_refuses_bad_ids(eg_lib):
     gid = np.repeat(np.arange(G), np.diff(eoff.astype(np.int64)))
     us = (src.astype(np.uint64) + voff[:-1].astype(np.uint64)[gid]).astype(np.uint32)
     assert np.array_equal(out, np.bincount(us, minlength=int(Vs.sum())).astype(np.uint32))
+
+
+def test_one_launch_build_batch_with_edgeless_graphs(eg_lib):
+    """Graphs without edges (repeated record offsets, one-vertex graphs) inside a batch: the move of
+    ids to the union skips them, and the one-launch build equals the per-pass build and the oracle."""
+    import endgraph_gb300 as eg
+    Vs = np.array([1, 500, 1, 1, 3000, 7, 2000, 1], np.uint32)
+    Es = np.array([0, 4000, 0, 0, 20000, 0, 9000, 0], np.uint64)
+    parts = [rmat_graph(int(v), int(e), 300 + i) if e else (np.zeros(0, np.uint32), np.zeros(0, np.uint32), None)
+             for i, (v, e) in enumerate(zip(Vs, Es))]
+    eoff = np.zeros(len(Vs) + 1, np.uint64)
+    eoff[1:] = np.cumsum(Es)
+    src = np.concatenate([p[0] for p in parts]).astype(np.uint32)
+    dst = np.concatenate([p[1] for p in parts]).astype(np.uint32)
+    recs = eg.pack_edges(src, dst)
+    with eg.Graph() as g:
+        g.set_option(eg.EG_OPT_BUILD_LAUNCH, 0)
+        g.load_graph_batch(recs, eoff, Vs)
+        per_pass = _structure(g)
+        g.set_option(eg.EG_OPT_BUILD_LAUNCH, 1)
+        g.load_graph_batch(recs, eoff, Vs)
+        one = _structure(g)
+        voff, _ = g.graph_batch()
+    _assert_same(per_pass, one)
+    gid = np.repeat(np.arange(len(Vs)), Es.astype(np.int64))
+    base = voff[:-1].astype(np.uint64)[gid]
+    _assert_oracle(one, (src.astype(np.uint64) + base).astype(np.uint32),
+                   (dst.astype(np.uint64) + base).astype(np.uint32), None, int(Vs.sum()))
