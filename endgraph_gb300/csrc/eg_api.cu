@@ -61,6 +61,7 @@ int init_handle(eg_graph* g, const eg_config* cfg) {
     }
     EG_TRY(g->err.reserve(64));
     EG_CUDA(cudaMemsetAsync(g->err.ptr, 0, 64, g->stream));
+    EG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&g->eng.host_words), 64, cudaHostAllocDefault));
     return EG_OK;
 }
 
@@ -71,6 +72,7 @@ void free_handle(eg_graph* g) {
     g->prof.clear();
     free_batch_state(g);
     if (g->pinned) cudaFreeHost(g->pinned);
+    if (g->eng.host_words) cudaFreeHost(g->eng.host_words);
     if (g->copy_stream) {
         cudaStreamSynchronize(g->copy_stream);
         cudaStreamDestroy(g->copy_stream);

@@ -121,7 +121,7 @@ struct EngineState {
     uint64_t pull_nchunks = 0;
     bool pull_ready = false;
     bool pr_ready = false;  // pr_new_id / pr_adj match the built CSC
-    DevBuf host_pinned_dummy;
+    uint64_t* host_words = nullptr;  // pinned host block for the per-level readbacks of counters
 };
 
 }  // namespace eg

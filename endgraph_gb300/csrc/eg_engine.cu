@@ -584,9 +584,10 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
                                            s.q0.as<uint32_t>());
         EG_CHECK_LAUNCH("k_bfs_root");
     }
-    uint32_t root_deg = 0;
-    EG_CUDA(cudaMemcpyAsync(&root_deg, g->outdeg.as<uint32_t>() + root, 4, cudaMemcpyDeviceToHost, g->stream));
+    uint32_t* hroot = reinterpret_cast<uint32_t*>(s.host_words + 3);  // pinned
+    EG_CUDA(cudaMemcpyAsync(hroot, g->outdeg.as<uint32_t>() + root, 4, cudaMemcpyDeviceToHost, g->stream));
     EG_CUDA(cudaStreamSynchronize(g->stream));
+    const uint32_t root_deg = *hroot;
     uint32_t* qa = s.q0.as<uint32_t>();
     uint32_t* qb = s.q1.as<uint32_t>();
     uint64_t n = 1, reach = 1;
@@ -629,15 +630,11 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
                 k_bu_tail<<<(unsigned)g->num_sms * 8u, 256, 0, g->stream>>>(a);
                 EG_CHECK_LAUNCH("k_bu_tail");
             }
-            struct {
-                uint32_t n;
-                uint32_t pad;
-                unsigned long long act;
-            } h;
-            EG_CUDA(cudaMemcpyAsync(&h, d_nout, 16, cudaMemcpyDeviceToHost, g->stream));
+            uint64_t* hw = s.host_words;  // pinned: queue length, active out-edges
+            EG_CUDA(cudaMemcpyAsync(hw, d_nout, 16, cudaMemcpyDeviceToHost, g->stream));
             EG_CUDA(cudaStreamSynchronize(g->stream));
-            nout = h.n;
-            act = h.act;
+            nout = (uint32_t)(hw[0] & 0xFFFFFFFFu);
+            act = hw[1];
             ++pulls;
         }
         EG_CUDA(cudaMemsetAsync(front, 0, bm_bytes, g->stream));

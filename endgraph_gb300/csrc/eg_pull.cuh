@@ -137,18 +137,14 @@ static int push_level(eg_graph* g, const Op& op, uint32_t* q, uint64_t n, uint32
         k_push<Op><<<kPersistentGrid, kPushThreads, 0, g->stream>>>(op, a);
         EG_CHECK_LAUNCH(name);
     }
-    struct {
-        uint32_t n;
-        uint32_t pad;
-        unsigned long long act;
-    } h;
-    uint64_t T = 0;
-    EG_CUDA(cudaMemcpyAsync(&h, d_nout, 16, cudaMemcpyDeviceToHost, g->stream));
-    EG_CUDA(cudaMemcpyAsync(&T, ipref + nitems, 8, cudaMemcpyDeviceToHost, g->stream));
+    // queue length, active out-edges and the level's edge total, into pinned host words
+    uint64_t* hw = s.host_words;
+    EG_CUDA(cudaMemcpyAsync(hw, d_nout, 16, cudaMemcpyDeviceToHost, g->stream));
+    EG_CUDA(cudaMemcpyAsync(hw + 2, ipref + nitems, 8, cudaMemcpyDeviceToHost, g->stream));
     EG_CUDA(cudaStreamSynchronize(g->stream));
-    *n_out_host = h.n;
-    if (edges_host) *edges_host = T;
-    if (act_edges_host) *act_edges_host = h.act;
+    *n_out_host = (uint32_t)(hw[0] & 0xFFFFFFFFu);
+    if (edges_host) *edges_host = hw[2];
+    if (act_edges_host) *act_edges_host = hw[1];
     return EG_OK;
 }
 
