@@ -61,7 +61,7 @@ int init_handle(eg_graph* g, const eg_config* cfg) {
     }
     EG_TRY(g->err.reserve(64));
     EG_CUDA(cudaMemsetAsync(g->err.ptr, 0, 64, g->stream));
-    EG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&g->eng.host_words), 64, cudaHostAllocDefault));
+    EG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&g->eng.host_words), 256, cudaHostAllocDefault));
     return EG_OK;
 }
 
@@ -73,6 +73,8 @@ void free_handle(eg_graph* g) {
     free_batch_state(g);
     if (g->pinned) cudaFreeHost(g->pinned);
     if (g->eng.host_words) cudaFreeHost(g->eng.host_words);
+    if (g->eng.bfs_exec) cudaGraphExecDestroy(g->eng.bfs_exec);
+    if (g->eng.bfs_graph) cudaGraphDestroy(g->eng.bfs_graph);
     if (g->copy_stream) {
         cudaStreamSynchronize(g->copy_stream);
         cudaStreamDestroy(g->copy_stream);

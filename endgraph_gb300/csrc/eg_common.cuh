@@ -121,7 +121,13 @@ struct EngineState {
     uint64_t pull_nchunks = 0;
     bool pull_ready = false;
     bool pr_ready = false;  // pr_new_id / pr_adj match the built CSC
-    uint64_t* host_words = nullptr;  // pinned host block for the per-level readbacks of counters
+    uint64_t* host_words = nullptr;  // pinned host block (256 bytes) for the readbacks of counters
+    // single-root BFS replayed as a CUDA graph (eg_engine.cu): the instantiated graph, its state
+    // words on the device and what it was built for
+    cudaGraphExec_t bfs_exec = nullptr;
+    cudaGraph_t bfs_graph = nullptr;
+    std::vector<uint64_t> bfs_key;
+    DevBuf bfs_state;
 };
 
 }  // namespace eg

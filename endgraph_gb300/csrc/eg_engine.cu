@@ -26,13 +26,14 @@ struct BfsOp {  // toolkits/bfs.cpp:52-58: first visitor of dst becomes its pare
     uint32_t* level;
     uint32_t* parent;
     uint32_t next_level;
+    const uint32_t* next_level_dev = nullptr;  // a replayed graph reads the level number here
     __device__ uint32_t payload(uint32_t) const { return 0; }
     __device__ bool relax(uint32_t u, uint32_t, uint32_t w, uint64_t) const {
         const unsigned long long bit = 1ull << (w & 63);
         unsigned long long* word = visited + (w >> 6);
         if (__ldcg(word) & bit) return false;
         if (atomicOr(word, bit) & bit) return false;
-        if (level) level[w] = next_level;
+        if (level) level[w] = next_level_dev ? __ldcg(next_level_dev) : next_level;
         if (parent) parent[w] = u;
         atomicOr(next_front + (w >> 6), bit);
         return true;
@@ -65,6 +66,7 @@ struct BuArgs {
     const uint32_t* deg;
     unsigned long long* seg;  // (segment << 32) | compressed entry
     uint32_t* nseg;
+    const uint32_t* next_level_dev = nullptr;  // a replayed graph reads the level number here
 };
 
 __device__ __forceinline__ bool bu_in_front(const BuArgs& a, uint32_t u) {
@@ -73,7 +75,7 @@ __device__ __forceinline__ bool bu_in_front(const BuArgs& a, uint32_t u) {
 __device__ __forceinline__ bool bu_claim(const BuArgs& a, uint32_t v, uint32_t par) {
     const unsigned long long bit = 1ull << (v & 63);
     if (atomicOr(a.visited + (v >> 6), bit) & bit) return false;  // another entry of v won
-    if (a.level) a.level[v] = a.next_level;
+    if (a.level) a.level[v] = a.next_level_dev ? __ldcg(a.next_level_dev) : a.next_level;
     if (a.parent) a.parent[v] = par;
     atomicOr(a.next_front + (v >> 6), bit);
     return true;
@@ -499,6 +501,217 @@ __global__ void k_sssp_root(float* dist, uint32_t root, uint32_t* q) {
 
 
 // ---------------------------------------------------------------------------------------------
+// Single-root BFS replayed as one CUDA graph with device-side control flow (EG_OPT_CUDA_GRAPH): a
+// WHILE conditional node whose body runs two levels (the even one from queue 0 and frontier bitmap
+// 0 into queue 1 and bitmap 1, the odd one back).  Each level is a one-thread kernel that arms one
+// of two IF conditional nodes — the push (scan of the queued lists' lengths, rank-balanced
+// expansion) or the dense step (early-exit head and tail) — or neither once the frontier is empty,
+// then a one-thread kernel that moves the level's counters into the state; the odd level's also
+// sets the loop condition.  No host round trip per level; the graph is built once per handle and
+// structure and replayed for every root.  A traversal deeper than kBfsGraphLevels continues in the
+// host loop from the state the graph leaves.
+constexpr uint32_t kBfsGraphLevels = 4096;
+
+struct BfsGraphState {
+    uint32_t n;           // frontier length of the next level
+    uint32_t lvl;         // levels done
+    uint32_t next_level;  // level number of the vertices the running level reaches
+    uint32_t ran;         // the running level was armed
+    unsigned long long act;    // out-edges of the frontier
+    unsigned long long reach;  // vertices reached
+    unsigned long long total;  // out-edges of the reached vertices
+    uint64_t scan_total;       // the push scan's edge total
+    uint32_t pushes, pulls;
+    uint32_t nout, pad0;       // the running level's queue length and out-edges
+    unsigned long long nact;
+    uint32_t nseg, pad1;       // the dense step's segments
+};
+
+static_assert(sizeof(BfsGraphState) <= 256, "the state is read back through the 256-byte pinned block");
+
+__global__ void k_bfsg_init(BfsGraphState* st, const uint32_t* __restrict__ outdeg, uint32_t root) {
+    const unsigned long long d = outdeg[root];
+    st->n = 1;
+    st->lvl = 0;
+    st->next_level = 1;
+    st->ran = 0;
+    st->act = d;
+    st->reach = 1;
+    st->total = d;
+    st->scan_total = 0;
+    st->pushes = st->pulls = 0;
+    st->nout = 0;
+    st->nact = 0;
+    st->nseg = 0;
+}
+
+// core/graph.hpp:1484-1491 (Gemini's switch) on the device: sparse iff the frontier's out-edges < E/div
+__global__ void k_bfsg_decide(BfsGraphState* st, cudaGraphConditionalHandle h_push, cudaGraphConditionalHandle h_pull,
+                              unsigned long long dense_min, int direction, int has_csc) {
+    const bool go = st->n > 0 && st->lvl < kBfsGraphLevels;
+    const bool dense = go && (direction == 2 || (direction == 0 && has_csc && st->act >= dense_min));
+    st->ran = go ? 1u : 0u;
+    st->next_level = st->lvl + 1;
+    st->nout = 0;
+    st->nact = 0;
+    st->nseg = 0;
+    if (go) {
+        if (dense) ++st->pulls;
+        else ++st->pushes;
+    }
+    cudaGraphSetConditional(h_push, go && !dense ? 1u : 0u);
+    cudaGraphSetConditional(h_pull, dense ? 1u : 0u);
+}
+
+__global__ void k_bfsg_post(BfsGraphState* st, cudaGraphConditionalHandle h_loop, int odd) {
+    if (st->ran) {
+        st->n = st->nout;
+        st->act = st->nact;
+        st->reach += st->nout;
+        st->total += st->nact;
+        ++st->lvl;
+    }
+    if (odd) cudaGraphSetConditional(h_loop, st->n > 0 && st->lvl < kBfsGraphLevels ? 1u : 0u);
+}
+
+// the key a built graph is valid for: sizes, switch settings and every buffer it was captured with
+static std::vector<uint64_t> bfs_graph_key(eg_graph* g) {
+    EngineState& s = g->eng;
+    auto p = [](const void* x) { return (uint64_t)(uintptr_t)x; };
+    return {g->V, g->E, g->ncompressed, (uint64_t)g->partitions, (uint64_t)g->dense_div, (uint64_t)g->bfs_direction,
+            (uint64_t)g->built_csc, p(g->csr_off.ptr), p(g->csr_adj.ptr), p(g->csc_adj.ptr), p(g->cidx.ptr),
+            p(g->cvert.ptr), p(g->outdeg.ptr), p(s.q0.ptr), p(s.q1.ptr), p(s.bm_visit.ptr), p(s.bm_next.ptr),
+            p(s.bm_front.ptr), p(s.vals0.ptr), p(s.vals1.ptr), p(s.qdeg.ptr), p(s.chunk_item.ptr), p(s.bu_seg.ptr),
+            p(g->scan.desc.ptr), p(g->scan.counter.ptr), p(g->err.ptr), p(s.bfs_state.ptr)};
+}
+
+static int build_bfs_graph(eg_graph* g) {
+    EngineState& s = g->eng;
+    const uint32_t V = g->V;
+    const int P = g->partitions;
+    const uint64_t max_items = (uint64_t)V * P;
+    const uint64_t max_tiles = (max_items + kScanTile - 1) / kScanTile + 1;
+    EG_TRY(g->scan.desc.reserve(max_tiles * sizeof(uint64_t)));
+    EG_TRY(g->scan.counter.reserve(16));
+    EG_TRY(s.bfs_state.reserve(sizeof(BfsGraphState)));
+    std::vector<uint64_t> key = bfs_graph_key(g);
+    if (s.bfs_exec && key == s.bfs_key) return EG_OK;
+    if (s.bfs_exec) cudaGraphExecDestroy(s.bfs_exec);
+    if (s.bfs_graph) cudaGraphDestroy(s.bfs_graph);
+    s.bfs_exec = nullptr;
+    s.bfs_graph = nullptr;
+    BfsGraphState* st = s.bfs_state.as<BfsGraphState>();
+    uint32_t* q[2] = {s.q0.as<uint32_t>(), s.q1.as<uint32_t>()};
+    unsigned long long* F[2] = {s.bm_next.as<unsigned long long>(), s.bm_front.as<unsigned long long>()};
+    unsigned long long* visit = s.bm_visit.as<unsigned long long>();
+    uint32_t* d_level = s.vals0.as<uint32_t>();
+    uint32_t* d_parent = s.vals1.as<uint32_t>();
+    const size_t bm_bytes = sizeof(uint64_t) * (V / 64 + 1);
+    const unsigned long long dense_min = g->E / (uint64_t)g->dense_div;
+    // captured on a stream of its own, so that nothing else the caller queued is recorded
+    cudaStream_t cs = nullptr;
+    EG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    struct StreamGuard {
+        cudaStream_t s;
+        ~StreamGuard() { cudaStreamDestroy(s); }
+    } guard{cs};
+    cudaGraph_t G = nullptr;
+    EG_CUDA(cudaGraphCreate(&G, 0));
+    s.bfs_graph = G;
+    cudaGraphConditionalHandle h_loop;
+    EG_CUDA(cudaGraphConditionalHandleCreate(&h_loop, G, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = h_loop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    EG_CUDA(cudaGraphAddNode(&wnode, G, nullptr, nullptr, 0, &wp));
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    cudaGraphConditionalHandle h_push[2], h_pull[2];
+    for (int k = 0; k < 2; ++k) {
+        EG_CUDA(cudaGraphConditionalHandleCreate(&h_push[k], body, 0, 0));
+        EG_CUDA(cudaGraphConditionalHandleCreate(&h_pull[k], body, 0, 0));
+    }
+    // an IF node after the capture's current dependencies; returns its (empty) body graph
+    auto add_if = [&](cudaGraphConditionalHandle h, cudaGraph_t* out) -> int {
+        cudaStreamCaptureStatus cst;
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        const cudaGraphEdgeData* ed = nullptr;
+        size_t nd = 0;
+        EG_CUDA(cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, &ed, &nd));
+        cudaGraphNodeParams ip = {};
+        ip.type = cudaGraphNodeTypeConditional;
+        ip.conditional.handle = h;
+        ip.conditional.type = cudaGraphCondTypeIf;
+        ip.conditional.size = 1;
+        cudaGraphNode_t node;
+        EG_CUDA(cudaGraphAddNode(&node, cg, deps, ed, nd, &ip));
+        *out = ip.conditional.phGraph_out[0];
+        EG_CUDA(cudaStreamUpdateCaptureDependencies(cs, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        return EG_OK;
+    };
+    cudaGraph_t push_body[2], pull_body[2];
+    EG_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < 2; ++k) {
+        k_bfsg_decide<<<1, 1, 0, cs>>>(st, h_push[k], h_pull[k], dense_min, g->bfs_direction, g->built_csc ? 1 : 0);
+        EG_TRY(add_if(h_push[k], &push_body[k]));
+        EG_TRY(add_if(h_pull[k], &pull_body[k]));
+        k_bfsg_post<<<1, 1, 0, cs>>>(st, h_loop, k);
+    }
+    cudaGraph_t captured = nullptr;
+    EG_CUDA(cudaStreamEndCapture(cs, &captured));
+    const unsigned scan_grid = (unsigned)std::min<uint64_t>(max_tiles, (uint64_t)g->num_sms * 8u);
+    for (int k = 0; k < 2; ++k) {
+        // push: queue q[k] -> q[k^1], new frontier bits in F[k^1]; F[k] cleared for the level after
+        EG_CUDA(cudaStreamBeginCaptureToGraph(cs, push_body[k], nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        EG_CUDA(cudaMemsetAsync(g->scan.desc.ptr, 0, max_tiles * sizeof(uint64_t), cs));
+        EG_CUDA(cudaMemsetAsync(g->scan.counter.ptr, 0, 4, cs));
+        uint64_t* ipref = s.qdeg.as<uint64_t>();
+        LoadItemLen ld{q[k], P, (uint64_t)V + 1, g->csr_off.as<uint64_t>()};
+        EpiItemRank ep{ipref, s.chunk_item.as<uint32_t>()};
+        k_scan<<<scan_grid, kScanThreads, 0, cs>>>(ld, ep, max_items, g->scan.desc.as<uint64_t>(),
+                                                   g->scan.counter.as<uint32_t>(), g->err.as<int>(), &st->scan_total,
+                                                   kLookbackSpinCap, &st->n, (uint32_t)P);
+        PushArgs a;
+        a.q = q[k];
+        a.nitems = 0;
+        a.n_dev = &st->n;
+        a.total_dev = &st->scan_total;
+        a.P = P;
+        a.stride = (uint64_t)V + 1;
+        a.off = g->csr_off.as<uint64_t>();
+        a.adj = g->csr_adj.as<uint32_t>();
+        a.w = g->csr_w.as<float>();
+        a.ipref = ipref;
+        a.chunk_item = s.chunk_item.as<uint32_t>();
+        a.q_out = q[k ^ 1];
+        a.n_out = &st->nout;
+        a.act_edges = &st->nact;
+        a.deg = g->outdeg.as<uint32_t>();
+        BfsOp op{visit, F[k ^ 1], d_level, d_parent, 0u, &st->next_level};
+        k_push<BfsOp><<<kPersistentGrid, kPushThreads, 0, cs>>>(op, a);
+        EG_CUDA(cudaMemsetAsync(F[k], 0, bm_bytes, cs));
+        EG_CUDA(cudaStreamEndCapture(cs, &captured));
+        // dense step: every unvisited destination looks for a parent in F[k]
+        EG_CUDA(cudaStreamBeginCaptureToGraph(cs, pull_body[k], nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        if (g->built_csc) {
+            BuArgs ba{g->csc_adj.as<uint32_t>(), g->cidx.as<uint64_t>(), g->cvert.as<uint32_t>(), g->ncompressed - 1, V,
+                      F[k], visit, F[k ^ 1], d_level, d_parent, 0u, q[k ^ 1], &st->nout, &st->nact,
+                      g->outdeg.as<uint32_t>(), s.bu_seg.as<unsigned long long>(), &st->nseg, &st->next_level};
+            k_bu_head<<<grid_for(ba.nitems, 256, (unsigned)g->num_sms * 8u), 256, 0, cs>>>(ba);
+            k_bu_tail<<<(unsigned)g->num_sms * 8u, 256, 0, cs>>>(ba);
+        }
+        EG_CUDA(cudaMemsetAsync(F[k], 0, bm_bytes, cs));
+        EG_CUDA(cudaStreamEndCapture(cs, &captured));
+    }
+    EG_CUDA(cudaGraphInstantiate(&s.bfs_exec, G, 0));
+    s.bfs_key = key;
+    return EG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
 int run_pagerank(eg_graph* g, int iterations, float damping, float* out, int where) {
     if (!g->built_csc) { set_error("eg_pagerank: CSC not built"); return EG_ERR_STATE; }
     if (iterations < 0) { set_error("eg_pagerank: iterations must be >= 0"); return EG_ERR_INVALID; }
@@ -584,22 +797,49 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
                                            s.q0.as<uint32_t>());
         EG_CHECK_LAUNCH("k_bfs_root");
     }
-    uint32_t* hroot = reinterpret_cast<uint32_t*>(s.host_words + 3);  // pinned
-    EG_CUDA(cudaMemcpyAsync(hroot, g->outdeg.as<uint32_t>() + root, 4, cudaMemcpyDeviceToHost, g->stream));
-    EG_CUDA(cudaStreamSynchronize(g->stream));
-    const uint32_t root_deg = *hroot;
-    uint32_t* qa = s.q0.as<uint32_t>();
-    uint32_t* qb = s.q1.as<uint32_t>();
-    uint64_t n = 1, reach = 1;
-    unsigned long long active_edges = root_deg, total_edges = root_deg;
-    uint32_t lvl = 0;
-    int pushes = 0, pulls = 0;
     if (g->built_csc) {
         // segment list of the dense step: at most one segment per entry with more than kBuHead
         // in-edges plus one per kBuSeg edges
         const uint64_t nitems = g->ncompressed - 1;
         const uint64_t heavy = std::min<uint64_t>(nitems, g->E / (kBuHead + 1));
         EG_TRY(s.bu_seg.reserve(sizeof(unsigned long long) * (heavy + g->E / kBuSeg + 2)));
+    }
+    uint32_t* qa = s.q0.as<uint32_t>();
+    uint32_t* qb = s.q1.as<uint32_t>();
+    uint64_t n = 1, reach = 1;
+    unsigned long long active_edges = 0, total_edges = 0;
+    uint32_t lvl = 0;
+    int pushes = 0, pulls = 0;
+    if (g->use_cuda_graph) {
+        // the whole level loop as one graph replay; the state it leaves says where it stopped
+        EG_TRY(build_bfs_graph(g));
+        BfsGraphState* st = s.bfs_state.as<BfsGraphState>();
+        k_bfsg_init<<<1, 1, 0, g->stream>>>(st, g->outdeg.as<uint32_t>(), root);
+        EG_CHECK_LAUNCH("k_bfsg_init");
+        {
+            Timed t(&g->prof, g->stream, "bfs_graph");
+            EG_CUDA(cudaGraphLaunch(s.bfs_exec, g->stream));
+        }
+        BfsGraphState* hs = reinterpret_cast<BfsGraphState*>(s.host_words);  // pinned
+        EG_CUDA(cudaMemcpyAsync(hs, st, sizeof(BfsGraphState), cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaStreamSynchronize(g->stream));
+        EG_TRY(check_device_error(g, "eg_bfs"));
+        n = hs->n;
+        lvl = hs->lvl;
+        reach = hs->reach;
+        active_edges = hs->act;
+        total_edges = hs->total;
+        pushes = (int)hs->pushes;
+        pulls = (int)hs->pulls;
+        if (lvl & 1) {  // level lvl reads queue lvl & 1 and frontier bitmap lvl & 1
+            std::swap(qa, qb);
+            std::swap(front, next_front);
+        }
+    } else {
+        uint32_t* hroot = reinterpret_cast<uint32_t*>(s.host_words + 3);  // pinned
+        EG_CUDA(cudaMemcpyAsync(hroot, g->outdeg.as<uint32_t>() + root, 4, cudaMemcpyDeviceToHost, g->stream));
+        EG_CUDA(cudaStreamSynchronize(g->stream));
+        active_edges = total_edges = *hroot;
     }
     while (n > 0) {
         // core/graph.hpp:1484-1491 (Gemini's switch): sparse iff the frontier's out-edges < E / div

@@ -188,6 +188,56 @@ def test_bfs_directions(eg_lib, direction, P):
                 assert run["push"] == 0
 
 
+@pytest.mark.parametrize("P", [1, 2])
+def test_bfs_graph_replay(eg_lib, P):
+    """Single-root BFS replayed as one CUDA graph (a WHILE conditional node over the levels, the
+    push/pull choice made on the device by IF conditional nodes) gives the oracle's levels and
+    valid parents in every direction mode, for several roots on one captured graph and after a
+    rebuild, and takes both directions as the host loop does."""
+    import endgraph_gb300 as eg
+    V, E = 1 << 16, 1 << 20
+    src, dst, _ = rmat_graph(V, E, 5)
+    csr = oracle.build_csr(src, dst, None, V, np.array([0, V], np.uint32))
+    with _graph(eg_lib, P=P) as g:
+        g.load_directed(eg.pack_edges(src, dst), V)
+        g.set_option(eg.EG_OPT_CUDA_GRAPH, 1)
+        for direction in (0, 1, 2):
+            g.set_option(eg.EG_OPT_BFS_DIRECTION, direction)
+            for root in (int(src[0]), int(src[100]), 12345):
+                lv, par = g.bfs(root)
+                ref = oracle.bfs_levels(csr["off"][0], csr["adj"], V, root)
+                assert np.array_equal(lv, ref), (direction, root)
+                assert oracle.bfs_check_parents(csr["off"][0], csr["adj"], V, root, lv, par) == 0
+                run = g.last_run()
+                if direction == 0 and ref[ref != oracle.UNREACHED].max() > 2:
+                    assert run["push"] > 0 and run["pull"] > 0
+        # a rebuild (other buffers) captures a new graph
+        src2, dst2, _ = rmat_graph(V, E // 2, 6)
+        g.load_directed(eg.pack_edges(src2, dst2), V)
+        csr2 = oracle.build_csr(src2, dst2, None, V, np.array([0, V], np.uint32))
+        g.set_option(eg.EG_OPT_BFS_DIRECTION, 0)
+        lv, _ = g.bfs(int(src2[0]))
+        assert np.array_equal(lv, oracle.bfs_levels(csr2["off"][0], csr2["adj"], V, int(src2[0])))
+
+
+def test_bfs_graph_replay_deeper_than_one_replay(eg_lib):
+    """A chain of 5,000 vertices: the replay stops at its level cap (4,096) and the host loop
+    finishes the traversal from the state it left."""
+    import endgraph_gb300 as eg
+    n = 5000
+    rng = np.random.default_rng(3)
+    perm = rng.permutation(n).astype(np.uint32)
+    src, dst = perm[:-1], perm[1:]
+    with _graph(eg_lib) as g:
+        g.load_directed(eg.pack_edges(src, dst), n)
+        g.set_option(eg.EG_OPT_CUDA_GRAPH, 1)
+        lv, par = g.bfs(int(perm[0]))
+    want = np.empty(n, np.uint32)
+    want[perm] = np.arange(n, dtype=np.uint32)
+    assert np.array_equal(lv, want)
+    assert np.array_equal(par[perm[1:]], perm[:-1])
+
+
 @pytest.mark.parametrize("V,E,seed", CASES)
 def test_cc(eg_lib, V, E, seed):
     import endgraph_gb300 as eg
