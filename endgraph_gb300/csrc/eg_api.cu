@@ -834,7 +834,7 @@ int eg_set_option(eg_graph* g, int option, int64_t value) {
             g->dense_div = (int)value;
             return EG_OK;
         case EG_OPT_CUDA_GRAPH:
-            if (value < 0 || value > 1) break;
+            if (value < 0 || value > 3) break;
             g->use_cuda_graph = (int)value;
             return EG_OK;
         case EG_OPT_PULL_BLOCKS_PER_SM:

@@ -1014,7 +1014,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
     constexpr uint64_t kUnknownQueue = ~0ull;
     // pull gathers through the CSC sources renumbered by out-degree class (hot frontier words share
     // cache lines), with a renumbered copy of each frontier; on one graph with the host-driven loop
-    const bool renum = one_graph && !g->use_cuda_graph && g->batch_launch != 1 && g->E > 0 && want_relabel(g);
+    const bool renum = one_graph && !(g->use_cuda_graph & 1) && g->batch_launch != 1 && g->E > 0 && want_relabel(g);
     if (renum) {
         EG_TRY(setup_relabel(g));
         EG_TRY(b.wr0.reserve(8 * V + 8));
@@ -1218,7 +1218,7 @@ static int msbfs_core(eg_graph* g, uint32_t n_entries, int nbits, uint8_t* lev, 
         sweeps = (int)hw.levels;
         pushes = (int)hw.pushes;
         lvl = hw.levels;
-    } else if (g->use_cuda_graph) {
+    } else if (g->use_cuda_graph & 1) {
         // init + kGraphLevels levels replayed as one CUDA graph, each level choosing push or pull
         // on the device (k_cap_decide); levels after an empty frontier do nothing
         const bool key_ok = b.graph_exec && b.graph_V == V && b.graph_lev == (lev != nullptr) &&

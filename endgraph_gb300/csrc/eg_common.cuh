@@ -189,7 +189,7 @@ struct eg_graph {
     // engine options (eg_set_option)
     int bfs_direction = 0;  // 0: Gemini threshold switch, 1: push only, 2: pull only
     int dense_div = 20;     // sparse iff active_edges < E / dense_div (core/graph.hpp:1491)
-    int use_cuda_graph = 0; // batched BFS: replay the level loop as one captured CUDA graph
+    int use_cuda_graph = 0; // bit 0: batched BFS level loop as a captured graph; bit 1: single-root BFS
     int batch_launch = 0;   // batched BFS: 1 runs every level inside one persistent launch
     int batch_div = 0;      // batched BFS switch divisor; 0: the same as dense_div
     int build_launch = 1;   // 1: a one-partition build runs as one persistent cooperative launch

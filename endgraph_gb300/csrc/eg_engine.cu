@@ -810,7 +810,7 @@ int run_bfs(eg_graph* g, uint32_t root, uint32_t* level, uint32_t* parent, int w
     unsigned long long active_edges = 0, total_edges = 0;
     uint32_t lvl = 0;
     int pushes = 0, pulls = 0;
-    if (g->use_cuda_graph) {
+    if (g->use_cuda_graph & 2) {
         // the whole level loop as one graph replay; the state it leaves says where it stopped
         EG_TRY(build_bfs_graph(g));
         BfsGraphState* st = s.bfs_state.as<BfsGraphState>();

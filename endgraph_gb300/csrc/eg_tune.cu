@@ -138,7 +138,7 @@ int eg_autotune(eg_graph* g, const uint32_t* sample_roots, int nroots, eg_tuning
     const int bdivs[] = {20, 10, 40, 5};
     for (int cg = 0; cg <= 1; ++cg) {
         for (int d : bdivs) {
-            g->use_cuda_graph = cg;
+            g->use_cuda_graph = (g->use_cuda_graph & 2) | cg;
             g->batch_div = d;
             EG_TRY(run_msbfs(g, r64.data(), 64, nullptr, EG_HOST, nullptr));  // capture outside the timing
             double ms = 0;
@@ -150,7 +150,7 @@ int eg_autotune(eg_graph* g, const uint32_t* sample_roots, int nroots, eg_tuning
             }
         }
     }
-    g->use_cuda_graph = best_graph;
+    g->use_cuda_graph = (g->use_cuda_graph & 2) | best_graph;  // the single-root bit is not tuned
     g->batch_div = best_bdiv;
     out->cuda_graph = best_graph;
     out->batch_divisor = best_bdiv;

@@ -182,9 +182,10 @@ int eg_sssp(eg_graph* g, uint32_t root, float* dist, int where);
  * EG_OPT_CUDA_GRAPH: 1 replays the batched-BFS level loop (eg_msbfs, eg_msbfs_graphs) as one
  * captured CUDA graph of 16 levels, each choosing push or pull on the device from its frontier's
  * out-edges (the same switch as the host loop), instead of one host round trip per level; deeper
- * traversals continue from the host.  It also replays the single-root eg_bfs level loop as one
- * graph with device-side control flow (a WHILE conditional node over the levels, IF conditional
- * nodes for push or pull), up to 4,096 levels per replay. */
+ * traversals continue from the host (bit 1, value 1).  Bit 2 (value 2; 3 for both) replays the
+ * single-root eg_bfs level loop as one graph with device-side control flow (a WHILE conditional
+ * node over the levels, IF conditional nodes for push or pull), up to 4,096 levels per replay;
+ * eg_autotune sets bit 1 only. */
 enum {
     EG_OPT_BFS_DIRECTION = 1,
     EG_OPT_DENSE_DIVISOR = 2,

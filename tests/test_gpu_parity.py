@@ -200,7 +200,7 @@ def test_bfs_graph_replay(eg_lib, P):
     csr = oracle.build_csr(src, dst, None, V, np.array([0, V], np.uint32))
     with _graph(eg_lib, P=P) as g:
         g.load_directed(eg.pack_edges(src, dst), V)
-        g.set_option(eg.EG_OPT_CUDA_GRAPH, 1)
+        g.set_option(eg.EG_OPT_CUDA_GRAPH, 2)
         for direction in (0, 1, 2):
             g.set_option(eg.EG_OPT_BFS_DIRECTION, direction)
             for root in (int(src[0]), int(src[100]), 12345):
@@ -230,7 +230,7 @@ def test_bfs_graph_replay_deeper_than_one_replay(eg_lib):
     src, dst = perm[:-1], perm[1:]
     with _graph(eg_lib) as g:
         g.load_directed(eg.pack_edges(src, dst), n)
-        g.set_option(eg.EG_OPT_CUDA_GRAPH, 1)
+        g.set_option(eg.EG_OPT_CUDA_GRAPH, 3)
         lv, par = g.bfs(int(perm[0]))
     want = np.empty(n, np.uint32)
     want[perm] = np.arange(n, dtype=np.uint32)
