@@ -182,6 +182,7 @@ struct eg_graph {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t part_ready[8] = {};
     cudaEvent_t copy_gate = nullptr;
+    int pageable_direct = -1;  // the device reads pageable host memory at the link's rate (-1: not asked yet)
     // batched operators (eg_batch.cu): opaque state, dropped at every load/build
     void* batch = nullptr;
     bool edge_ids = false;   // the weight slot of each record holds the record's input index
