@@ -609,13 +609,37 @@ int load_file_impl(eg_graph* g, const char* path, uint32_t V, int edge_bytes, in
         close(fd);
         return st_load;
     }
-    // where the device reads pageable memory at the link's rate: the file's mapping, its pages
-    // touched by host threads, goes up in one copy
+    // where the device reads pageable memory at the link's rate: the file's mapping goes up in
+    // pieces, a helper thread touching the pages of piece i + 1 while piece i is copied
     if (bytes && pageable_at_link_rate(g)) {
         void* map = mmap(nullptr, (size_t)bytes, PROT_READ, MAP_SHARED, fd, 0);
         if (map != MAP_FAILED) {
-            touch_pages(static_cast<const uint8_t*>(map), 0, (size_t)bytes);
-            cudaError_t e = cudaMemcpyAsync(g->edges.ptr, map, (size_t)bytes, cudaMemcpyDefault, g->stream);
+            const uint8_t* src = static_cast<const uint8_t*>(map);
+            constexpr size_t kPiece = 2 * kIngestPiece;
+            const uint64_t npieces = (bytes + kPiece - 1) / kPiece;
+            std::atomic<uint64_t> touched{0};
+            std::atomic<bool> stop{false};
+            auto toucher = [&] {
+                for (uint64_t i = 0; i < npieces && !stop.load(std::memory_order_relaxed); ++i) {
+                    const size_t off = (size_t)(i * kPiece);
+                    touch_pages(src, off, (size_t)std::min<uint64_t>(kPiece, bytes - off));
+                    touched.store(i + 1, std::memory_order_release);
+                }
+            };
+            std::thread th;
+            try {
+                th = std::thread(toucher);
+            } catch (...) {
+                toucher();
+            }
+            cudaError_t e = cudaSuccess;
+            for (uint64_t i = 0; i < npieces && e == cudaSuccess; ++i) {
+                while (touched.load(std::memory_order_acquire) <= i) std::this_thread::yield();
+                const size_t off = (size_t)(i * kPiece), n = (size_t)std::min<uint64_t>(kPiece, bytes - off);
+                e = cudaMemcpyAsync(g->edges.as<uint8_t>() + off, src + off, n, cudaMemcpyDefault, g->stream);
+            }
+            stop.store(true, std::memory_order_relaxed);
+            if (th.joinable()) th.join();
             const cudaError_t e2 = cudaStreamSynchronize(g->stream);  // the mapping is read until here
             munmap(map, (size_t)bytes);
             close(fd);
