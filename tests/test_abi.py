@@ -43,6 +43,23 @@ def test_python_binding_covers_the_header(lib):
     assert declared_functions() <= set(eg.SIGNATURES)
 
 
+def test_python_constants_match_the_header():
+    """Every EG_OPT_*, EG_ERR_* and location constant the header defines has the same value in the
+    Python binding (a renumbered option would otherwise set another one silently)."""
+    import endgraph_gb300 as eg
+    text = open(os.path.join(ROOT, "include", "endgraph_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    consts = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(EG_(?:OPT|ERR)_\w+|EG_OK|EG_HOST|EG_DEVICE)\s*=\s*(-?\d+)", text)}
+    assert "EG_OPT_BUILD_LAUNCH" in consts and len(consts) >= 15
+    status = {k: v for k, v in consts.items() if k == "EG_OK" or k.startswith("EG_ERR_")}
+    assert {v: k for k, v in status.items()} == eg.STATUS  # status names by value
+    names = {k: v for k, v in consts.items() if k not in status}
+    missing = [k for k in names if not hasattr(eg, k)]
+    assert not missing, missing
+    wrong = {k: (v, getattr(eg, k)) for k, v in names.items() if getattr(eg, k) != v}
+    assert not wrong, wrong
+
+
 def test_argument_errors_without_gpu(lib):
     import endgraph_gb300 as eg
     out = np.zeros(4, np.uint32)
